@@ -1,0 +1,150 @@
+/*
+ * ssgpu.h -- C ABI of libssgpu.so, the GB300 exhaustive k-NN engine behind
+ * SimilaritySearch.jl's `searchbatch` / `allknn` path.
+ *
+ * Every entry point takes plain pointers and sizes; nothing crosses the
+ * boundary but C types.  Each call returns SSG_OK (0) or a negative status and
+ * never aborts; the text of the last failure is kept per index (or per thread
+ * for failures without an index) and read with ssg_last_error.
+ *
+ * Layout.  A Julia `Matrix{Float32}(d, n)` (column i = object i) is, byte for
+ * byte, a C row-major n x d array, so databases and query sets are passed as
+ * `n` rows of `ld` elements (ld >= dim, the column stride of a Julia view).
+ * Sketch databases (`Matrix{UInt64}(W, n)`) are n rows of W words.  Result
+ * matrices `(k, m)` are m rows of k: ids are 1-based UInt32, unfilled slots
+ * hold id 0 and +Inf, and every row is sorted by (distance, id), the order
+ * `KnnSorted` produces (src/pqueue/knnsorted.jl:68-101,140-168).
+ *
+ * Threading.  One handle owns one CUDA stream and a mutex: calls on a handle
+ * are serialised, distinct handles may be used from different threads.
+ */
+#ifndef SSGPU_H
+#define SSGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SSG_OK            0
+#define SSG_EINVAL       -1   /* bad argument: shapes, empty inputs, k out of range */
+#define SSG_ENOMEM       -2   /* device or pinned-host allocation failed            */
+#define SSG_ECUDA        -3   /* a CUDA runtime / kernel error                      */
+#define SSG_ETIMEOUT     -4   /* a bounded device-side wait gave up                 */
+#define SSG_EUNSUPPORTED -5   /* metric / element type / mode not supported         */
+
+/* ---- distances (SimilaritySearch.jl `Dist.*`) ----
+ * SQL2        Dist.SqL2        sum (x_i - q_i)^2            src/dist/vecs.jl:86,93-102
+ * L2          Dist.L2          sqrt(sum (x_i - q_i)^2)      src/dist/vecs.jl:52,59-67
+ * NORMCOSINE  Dist.NormCosine  1 - sum x_i q_i              src/dist/cos.jl:39,76-84
+ * COSINE      Dist.Cosine      1 - x.q / (|x| |q|)          src/dist/cos.jl:16,103
+ * IP          (new)            -sum x_i q_i  (NormCosine - 1, max inner product)
+ * HAMMING     Dist.Bits.Hamming  Float32(sum popcount(x_w xor q_w))  src/dist/bits.jl:10,18-25
+ * The Dist.CastF32 twins (src/dist/vecs-cast-f32.jl:76-93,148-189) are the
+ * float metrics over a non-Float32 element type: pass that element type and
+ * the library casts every element to Float32 on upload. */
+#define SSG_METRIC_SQL2        0
+#define SSG_METRIC_L2          1
+#define SSG_METRIC_NORMCOSINE  2
+#define SSG_METRIC_COSINE      3
+#define SSG_METRIC_IP          4
+#define SSG_METRIC_HAMMING     5
+
+/* ---- element types of host buffers ---- */
+#define SSG_ELEM_F32  0
+#define SSG_ELEM_U64  1   /* packed bit sketches, HAMMING only */
+#define SSG_ELEM_F64  2   /* CastF32 twins: cast to Float32 on upload */
+#define SSG_ELEM_F16  3
+#define SSG_ELEM_U8   4
+#define SSG_ELEM_I8   5
+
+/* ---- precision modes of the float metrics ----
+ * FP32: the plain method; results match ExhaustiveSearch on the same inputs
+ *       (distances within 1e-5 relative, ids equal outside near-tie bands).
+ * BF16: BF16 tensor-core distances over-fetching c*k candidates per query,
+ *       re-ranked in exact FP32 difference form (c = "overfetch" param).
+ * FP8:  FP8 e4m3 with a per-vector scale, same over-fetch and FP32 rerank. */
+#define SSG_PREC_FP32  0
+#define SSG_PREC_BF16  1
+#define SSG_PREC_FP8   2
+
+typedef struct ssg_index ssg_index;
+
+/* Builds a GPU index over `n` objects of `dim` elements (row stride `ld`)
+ * copied from host memory.  Replaces the construction of
+ * ExhaustiveSearch(dist, MatrixDatabase(X)) / ParallelExhaustiveSearch
+ * (src/exact/sequential-exhaustive.jl:18-21, src/exact/parallel-exhaustive.jl:26-29).
+ * For HAMMING, `dim` is the number of UInt64 words per sketch. */
+int ssg_create(int metric, int elem_type, int64_t dim, int64_t n,
+               const void *host_db, int64_t ld, int precision_mode, ssg_index **out);
+
+/* Same, from a database already in device memory (n rows of `ld` elements of
+ * `elem_type`); the library keeps its own copy. */
+int ssg_create_device(int metric, int elem_type, int64_t dim, int64_t n,
+                      const void *dev_db, int64_t ld, int precision_mode, ssg_index **out);
+
+/* k nearest neighbours of `m` queries (host rows of `dim` elements of the
+ * index's element type, contiguous) written to host out_ids / out_dists
+ * (m rows of k).  Replaces the matrix searchbatch! loop
+ * (src/SimilaritySearch.jl:331-348) over search(::ExhaustiveSearch)
+ * (src/exact/sequential-exhaustive.jl:68-80) and
+ * search(::ParallelExhaustiveSearch) (src/exact/parallel-exhaustive.jl:64-102).
+ * flags: reserved, pass 0. */
+int ssg_search(ssg_index *idx, const void *host_q, int64_t dim, int64_t m, int32_t k,
+               uint32_t *out_ids, float *out_dists, int32_t flags);
+
+/* Same as ssg_search with queries and results in device memory (results are
+ * written on the index's stream; the call returns once they are complete). */
+int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k,
+                      uint32_t *dev_ids, float *dev_dists, int32_t flags);
+
+/* All-vs-all k-NN over the indexed objects.  exclude_self == 0 keeps each
+ * object in its own result like allknn! (src/allknn.jl:66-110); exclude_self
+ * != 0 computes k+1 neighbours and drops the object itself (or the last one
+ * when the object is not among them).  Results are n rows of k. */
+int ssg_allknn(ssg_index *idx, int32_t k, int32_t exclude_self,
+               uint32_t *out_ids, float *out_dists);
+int ssg_allknn_device(ssg_index *idx, int32_t k, int32_t exclude_self,
+                      uint32_t *dev_ids, float *dev_dists);
+
+/* Appends `count` objects (host rows of `dim` elements, contiguous) with ids
+ * n+1 .. n+count.  Replaces append_items! / push_item!
+ * (src/exact/sequential-exhaustive.jl:33-47). */
+int ssg_append(ssg_index *idx, const void *host_rows, int64_t count);
+
+/* Re-scores and sorts candidate lists exactly (rerank!, src/rerank.jl:22-86):
+ * row j of ids (len entries, 1-based, 0 ends the list) is re-evaluated
+ * against query j with the index's metric in FP32 and sorted by
+ * (distance, id).  Host buffers; m rows. */
+int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
+               uint32_t *ids, float *dists);
+
+/* Tunables: "overfetch" (candidates per k in BF16/FP8 modes), "splits"
+ * (database splits per query tile, 0 = auto), "profile" (1 = time the main
+ * kernel with events), "max_cands".  Unknown keys return SSG_EINVAL. */
+int ssg_set_param(ssg_index *idx, const char *key, double value);
+/* Readable keys: the tunables plus "n", "dim", "metric", "precision",
+ * "main_kernel_ms" / "main_kernel_launches" (accumulated while profiling),
+ * "kernel_launches" (kernels launched by the last call), "device_bytes". */
+int ssg_get_param(ssg_index *idx, const char *key, double *value);
+
+/* Runs the index's work on `stream` (a cudaStream_t) instead of its own. */
+int ssg_set_stream(ssg_index *idx, void *stream);
+
+/* Copies the last error text (NUL terminated, truncated to len). idx may be
+ * NULL for failures of ssg_create*. Returns the full length of the text. */
+int ssg_last_error(ssg_index *idx, char *buf, int64_t len);
+
+/* Releases the index and its device memory. */
+void ssg_destroy(ssg_index *idx);
+
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int ssg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SSGPU_H */

@@ -1,0 +1,34 @@
+"""similaritysearch_gb300 -- GB300-native exhaustive k-NN behind SimilaritySearch.jl's API.
+
+Host-side mirror of the reference's ``searchbatch`` / ``allknn`` path over a
+GPU index (``GPUExhaustiveSearch``) whose work is done by libssgpu.so, the
+sm_103a CUDA library with the C ABI of ``include/ssgpu.h``.
+"""
+from . import _native
+from .db import AbstractDatabase, MatrixDatabase, VectorDatabase
+from .dist import Dist, PreMetric, evaluate
+from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,
+                    allknn, allknn_b, append_items_b, database, distance, distance_evaluations, index_b,
+                    push_item_b, rerank_b, search, searchbatch, searchbatch_b)
+from .log import LOG, InformativeLog, LogList, RecorderLog
+from .perf import macrorecall, recallscore
+from .pqueue import IdDist, KnnSorted, knnqueue
+
+# ParallelExhaustiveSearch and ExhaustiveSearch return the same results; on the
+# GPU both are the same index.
+GPUParallelExhaustiveSearch = GPUExhaustiveSearch
+
+__all__ = [
+    "AbstractDatabase", "MatrixDatabase", "VectorDatabase", "Dist", "PreMetric", "evaluate",
+    "ArgumentError", "GenericContext", "GPUExhaustiveSearch", "GPUParallelExhaustiveSearch",
+    "add_distance_evaluations", "allknn", "allknn_b", "append_items_b", "database", "distance",
+    "distance_evaluations", "index_b", "push_item_b", "rerank_b", "search", "searchbatch",
+    "searchbatch_b", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
+    "IdDist", "KnnSorted", "knnqueue",
+]
+
+
+def build(verbose: bool = False) -> str:
+    """Compiles libssgpu.so in-tree (nvcc, sm_103a)."""
+    from .build import build as _build
+    return _build(verbose=verbose)

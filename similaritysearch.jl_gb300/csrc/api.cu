@@ -1,0 +1,595 @@
+// api.cu -- the C ABI of libssgpu (declared in include/ssgpu.h).
+//
+// An index owns a device copy of the database, its CUDA stream, scratch
+// buffers and a last-error string.  Every entry point validates its arguments
+// the way the reference does (searchbatch! throws ArgumentError on an empty
+// query set or mismatched output shape, src/SimilaritySearch.jl:334-335;
+// allknn! asserts 0 < k <= n, src/allknn.jl:73-75) and returns a status code
+// instead of throwing.  Nothing here falls back to a CPU path: every result is
+// produced by the kernels in this library.
+#include "../../include/ssgpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+bool is_float_metric(int m) { return m >= SSG_METRIC_SQL2 && m <= SSG_METRIC_IP; }
+
+size_t elem_size(int e) {
+    switch (e) {
+        case SSG_ELEM_F32: return 4;
+        case SSG_ELEM_U64: return 8;
+        case SSG_ELEM_F64: return 8;
+        case SSG_ELEM_F16: return 2;
+        case SSG_ELEM_U8: return 1;
+        case SSG_ELEM_I8: return 1;
+        default: return 0;
+    }
+}
+
+}  // namespace
+
+struct ssg_index {
+    int metric = 0, elem = 0, prec = 0;
+    int64_t dim = 0, n = 0, cap = 0;
+    int device = 0;
+    DevBuf db;       // n x dim Float32 rows, or n x W UInt64 sketches
+    DevBuf db_norm;  // |x| per row (COSINE)
+    DevBuf qbuf, qnorm, qraw, cand, gheap, outbuf, stage;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::mutex mu;
+    char err[512] = "";
+    // tunables
+    int splits_param = 0;
+    double overfetch = 4.0;
+    int profile = 0;
+    // statistics
+    double main_ms = 0.0;
+    int64_t main_launches = 0;
+    int last_launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int fail(ssg_index *idx, int code, const char *fmt, ...) {
+    char *dst = idx ? idx->err : g_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(ssg_index *idx, cudaError_t e, const char *what) {
+    cudaGetLastError();  // clear the sticky-free error state of the last call
+    return fail(idx, e == cudaErrorMemoryAllocation ? SSG_ENOMEM : SSG_ECUDA, "%s: %s (%s)", what,
+                cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define SSG_CK(call, what)                                  \
+    do {                                                    \
+        cudaError_t _e = (call);                            \
+        if (_e != cudaSuccess) return cuda_fail(idx, _e, what); \
+    } while (0)
+
+// Uploads `rows` rows (row stride `ld` elements of `elem`) from host or device
+// memory into dst as contiguous Float32 (or UInt64) rows of `dim`.
+int upload_rows(ssg_index *idx, void *dst, const void *src, int64_t rows, int64_t ld, bool src_device) {
+    if (rows == 0) return SSG_OK;
+    const size_t es = elem_size(idx->elem);
+    const cudaMemcpyKind kind = src_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const bool cast = (idx->elem != SSG_ELEM_F32 && idx->elem != SSG_ELEM_U64);
+    void *target = dst;
+    if (cast) {
+        SSG_CK(idx->stage.ensure(size_t(rows) * idx->dim * es), "allocating the cast staging buffer");
+        target = idx->stage.p;
+    }
+    if (ld == idx->dim) {
+        SSG_CK(cudaMemcpyAsync(target, src, size_t(rows) * idx->dim * es, kind, idx->stream), "copying rows");
+    } else {
+        SSG_CK(cudaMemcpy2DAsync(target, size_t(idx->dim) * es, src, size_t(ld) * es,
+                                 size_t(idx->dim) * es, size_t(rows), kind, idx->stream),
+               "copying strided rows");
+    }
+    if (cast) {
+        SSG_CK(ssg::launch_cast_f32(idx->stage.p, idx->elem, rows * idx->dim, static_cast<float *>(dst),
+                                    idx->stream, &idx->last_launches),
+               "casting rows to Float32");
+    }
+    return SSG_OK;
+}
+
+int ensure_db_capacity(ssg_index *idx, int64_t rows) {
+    if (rows <= idx->cap) return SSG_OK;
+    int64_t newcap = std::max<int64_t>(rows, idx->cap + idx->cap / 2);
+    const size_t row_bytes = size_t(idx->dim) * (idx->metric == SSG_METRIC_HAMMING ? 8 : 4);
+    void *p = nullptr;
+    SSG_CK(cudaMalloc(&p, size_t(newcap) * row_bytes), "allocating the database");
+    if (idx->n > 0) {
+        cudaError_t e = cudaMemcpyAsync(p, idx->db.p, size_t(idx->n) * row_bytes, cudaMemcpyDeviceToDevice,
+                                        idx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(idx->stream);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return cuda_fail(idx, e, "growing the database");
+        }
+    }
+    idx->db.release();
+    idx->db.p = p;
+    idx->db.bytes = size_t(newcap) * row_bytes;
+    if (idx->metric == SSG_METRIC_COSINE) {
+        void *np = nullptr;
+        SSG_CK(cudaMalloc(&np, size_t(newcap) * 4), "allocating database norms");
+        if (idx->n > 0) {
+            cudaError_t e = cudaMemcpyAsync(np, idx->db_norm.p, size_t(idx->n) * 4, cudaMemcpyDeviceToDevice,
+                                            idx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(idx->stream);
+            if (e != cudaSuccess) {
+                cudaFree(np);
+                return cuda_fail(idx, e, "growing database norms");
+            }
+        }
+        idx->db_norm.release();
+        idx->db_norm.p = np;
+        idx->db_norm.bytes = size_t(newcap) * 4;
+    }
+    idx->cap = newcap;
+    return SSG_OK;
+}
+
+int add_rows(ssg_index *idx, const void *src, int64_t rows, int64_t ld, bool src_device) {
+    int rc = ensure_db_capacity(idx, idx->n + rows);
+    if (rc) return rc;
+    const size_t row_bytes = size_t(idx->dim) * (idx->metric == SSG_METRIC_HAMMING ? 8 : 4);
+    void *dst = static_cast<char *>(idx->db.p) + size_t(idx->n) * row_bytes;
+    rc = upload_rows(idx, dst, src, rows, ld, src_device);
+    if (rc) return rc;
+    if (idx->metric == SSG_METRIC_COSINE) {
+        SSG_CK(ssg::launch_row_norms(static_cast<const float *>(dst), rows, idx->dim,
+                                     static_cast<float *>(idx->db_norm.p) + idx->n, idx->stream,
+                                     &idx->last_launches),
+               "computing database norms");
+    }
+    SSG_CK(cudaStreamSynchronize(idx->stream), "uploading the database");
+    idx->n += rows;
+    return SSG_OK;
+}
+
+int validate_create(int metric, int elem, int64_t dim, int64_t n, int64_t ld, int prec) {
+    if (metric < SSG_METRIC_SQL2 || metric > SSG_METRIC_HAMMING)
+        return fail(nullptr, SSG_EUNSUPPORTED, "unsupported metric code %d", metric);
+    if (elem_size(elem) == 0) return fail(nullptr, SSG_EUNSUPPORTED, "unsupported element type %d", elem);
+    if (metric == SSG_METRIC_HAMMING && elem != SSG_ELEM_U64)
+        return fail(nullptr, SSG_EUNSUPPORTED, "Hamming needs UInt64 sketches (element type %d given)", elem);
+    if (metric != SSG_METRIC_HAMMING && elem == SSG_ELEM_U64)
+        return fail(nullptr, SSG_EUNSUPPORTED, "float metrics need a numeric element type, not UInt64");
+    if (dim <= 0) return fail(nullptr, SSG_EINVAL, "dimension must be positive (got %lld)", (long long)dim);
+    if (metric == SSG_METRIC_HAMMING && dim > 32)
+        return fail(nullptr, SSG_EUNSUPPORTED, "Hamming sketches are limited to 32 words (2048 bits), got %lld",
+                    (long long)dim);
+    if (n < 0 || n >= (int64_t(1) << 32) - 1)
+        return fail(nullptr, SSG_EINVAL, "database length %lld out of range", (long long)n);
+    if (ld < dim) return fail(nullptr, SSG_EINVAL, "leading dimension %lld < dim %lld", (long long)ld, (long long)dim);
+    if (prec != SSG_PREC_FP32)
+        return fail(nullptr, SSG_EUNSUPPORTED, "precision mode %d is not available in this build", prec);
+    return SSG_OK;
+}
+
+int create_common(int metric, int elem, int64_t dim, int64_t n, const void *src, int64_t ld, int prec,
+                  ssg_index **out, bool src_device) {
+    if (!out) return fail(nullptr, SSG_EINVAL, "out pointer is NULL");
+    *out = nullptr;
+    int rc = validate_create(metric, elem, dim, n, ld, prec);
+    if (rc) return rc;
+    if (n > 0 && !src) return fail(nullptr, SSG_EINVAL, "database pointer is NULL");
+    ssg_index *idx = new ssg_index();
+    idx->metric = metric;
+    idx->elem = elem;
+    idx->prec = prec;
+    idx->dim = dim;
+    cudaError_t e = cudaGetDevice(&idx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&idx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&idx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&idx->ev1);
+    if (e != cudaSuccess) {
+        cuda_fail(nullptr, e, "creating the index stream");
+        ssg_destroy(idx);
+        return SSG_ECUDA;
+    }
+    idx->own_stream = true;
+    rc = add_rows(idx, src, n, ld, src_device);
+    if (rc) {
+        snprintf(g_err, sizeof g_err, "%s", idx->err);
+        ssg_destroy(idx);
+        return rc;
+    }
+    *out = idx;
+    return SSG_OK;
+}
+
+// Picks the number of database splits per query tile: enough blocks to fill
+// the GPU several times over, while every split stays long enough to amortise
+// its heap and the merge stays within one block's shared memory.
+int choose_splits(ssg_index *idx, int64_t m, int kk, int qpb) {
+    if (idx->splits_param > 0) return idx->splits_param;
+    const int64_t qtiles = (m + qpb - 1) / qpb;
+    const int64_t target = int64_t(4) * ssg::device_sm_count();
+    int64_t s = (target + qtiles - 1) / qtiles;
+    const int64_t min_len = std::max<int64_t>(1024, int64_t(8) * kk);
+    s = std::min<int64_t>(s, std::max<int64_t>(1, idx->n / min_len));
+    s = std::min<int64_t>(s, std::max<int64_t>(1, 8192 / kk));
+    return int(std::max<int64_t>(1, s));
+}
+
+// The search pipeline: scan (fused distances + top-k per split) then merge
+// and decode.  dq are device query rows (Float32 or UInt64), dqn their norms.
+int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+            uint32_t *d_ids, float *d_dists) {
+    const int take = k + (exclude_self ? 1 : 0);
+    const int kk = int(std::min<int64_t>(take, std::max<int64_t>(1, idx->n)));
+    const int qpb = (idx->metric == SSG_METRIC_HAMMING) ? 128 : 128;
+    const int splits = choose_splits(idx, m, kk, qpb);
+    const int64_t split_len = (idx->n + splits - 1) / splits;
+    // bound the candidate scratch to ~1 GiB by processing queries in chunks
+    const size_t per_query = size_t(splits) * kk * 8;
+    int64_t chunk = std::max<int64_t>(1, int64_t((size_t(1) << 30) / per_query));
+    chunk = std::min<int64_t>(chunk, m);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    const size_t qrow_bytes = size_t(idx->dim) * (idx->metric == SSG_METRIC_HAMMING ? 8 : 4);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        ssg::ScanArgs a{};
+        a.metric = idx->metric;
+        a.n = idx->n;
+        a.dim = idx->dim;
+        a.m = mc;
+        a.kk = kk;
+        a.splits = splits;
+        a.split_len = split_len;
+        a.cand = static_cast<uint64_t *>(idx->cand.p);
+        a.id_base = 0;
+        const void *qc = static_cast<const char *>(dq) + size_t(c0) * qrow_bytes;
+        size_t gh = idx->metric == SSG_METRIC_HAMMING ? ssg::hamming_gheap_bytes(a) : ssg::direct_gheap_bytes(a);
+        if (gh) {
+            SSG_CK(idx->gheap.ensure(gh), "allocating heap scratch");
+            a.gheap = static_cast<uint64_t *>(idx->gheap.p);
+        }
+        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
+        cudaError_t e;
+        if (idx->metric == SSG_METRIC_HAMMING) {
+            e = ssg::launch_hamming(a, static_cast<const uint64_t *>(idx->db.p), static_cast<const uint64_t *>(qc),
+                                    idx->stream, &idx->last_launches);
+        } else {
+            e = ssg::launch_direct_f32(a, static_cast<const float *>(idx->db.p),
+                                       static_cast<const float *>(idx->db_norm.p), static_cast<const float *>(qc),
+                                       dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches);
+        }
+        SSG_CK(e, "launching the scan kernel");
+        if (idx->profile) {
+            SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
+        }
+        ssg::FinalizeArgs f{};
+        f.cand = a.cand;
+        f.segs = splits;
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        SSG_CK(ssg::launch_finalize(f, idx->stream, &idx->last_launches), "launching the merge kernel");
+        if (idx->profile) {
+            SSG_CK(cudaEventSynchronize(idx->ev1), "timing the scan kernel");
+            float ms = 0.f;
+            SSG_CK(cudaEventElapsedTime(&ms, idx->ev0, idx->ev1), "timing the scan kernel");
+            idx->main_ms += ms;
+            idx->main_launches += 1;
+        }
+    }
+    return SSG_OK;
+}
+
+int prepare_queries(ssg_index *idx, const void *q, int64_t m, bool src_device, const void **dq, const float **dqn) {
+    const bool hamming = idx->metric == SSG_METRIC_HAMMING;
+    const size_t qbytes = size_t(m) * idx->dim * (hamming ? 8 : 4);
+    if (src_device && (idx->elem == SSG_ELEM_F32 || hamming)) {
+        *dq = q;
+    } else {
+        SSG_CK(idx->qbuf.ensure(qbytes), "allocating query staging");
+        int rc = upload_rows(idx, idx->qbuf.p, q, m, idx->dim, src_device);
+        if (rc) return rc;
+        *dq = idx->qbuf.p;
+    }
+    *dqn = nullptr;
+    if (idx->metric == SSG_METRIC_COSINE) {
+        SSG_CK(idx->qnorm.ensure(size_t(m) * 4), "allocating query norms");
+        SSG_CK(ssg::launch_row_norms(static_cast<const float *>(*dq), m, idx->dim,
+                                     static_cast<float *>(idx->qnorm.p), idx->stream, &idx->last_launches),
+               "computing query norms");
+        *dqn = static_cast<const float *>(idx->qnorm.p);
+    }
+    return SSG_OK;
+}
+
+int finish_call(ssg_index *idx, bool sync) {
+    SSG_CK(cudaGetLastError(), "launching");
+    if (sync) SSG_CK(cudaStreamSynchronize(idx->stream), "running the search");
+    return SSG_OK;
+}
+
+// Serialises calls on one handle and makes its device current.  Calls that
+// launch work pass `counts = true` to restart the per-call launch counter.
+struct Guard {
+    ssg_index *idx;
+    std::unique_lock<std::mutex> lk;
+    explicit Guard(ssg_index *i, bool counts = true) : idx(i), lk(i->mu) {
+        cudaSetDevice(i->device);
+        if (counts) i->last_launches = 0;
+    }
+};
+
+int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t k, uint32_t *ids,
+                  float *dists, int32_t flags, bool device) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (m <= 0) return fail(idx, SSG_EINVAL, "empty set of queries");
+    if (dim != idx->dim)
+        return fail(idx, SSG_EINVAL, "query dimension %lld does not match the index (%lld)", (long long)dim,
+                    (long long)idx->dim);
+    if (k <= 0) return fail(idx, SSG_EINVAL, "k must be positive (got %d)", k);
+    if (!q || !ids || !dists) return fail(idx, SSG_EINVAL, "NULL query or output pointer");
+    if (idx->n == 0) {
+        // An empty database leaves every slot at 0 / Inf32, as searchbatch does.
+        if (device) {
+            return fail(idx, SSG_EINVAL, "the index is empty");
+        }
+        for (int64_t i = 0; i < m * int64_t(k); ++i) { ids[i] = 0; dists[i] = INFINITY; }
+        return SSG_OK;
+    }
+    const void *dq;
+    const float *dqn;
+    int rc = prepare_queries(idx, q, m, device, &dq, &dqn);
+    if (rc) return rc;
+    uint32_t *d_ids = ids;
+    float *d_dists = dists;
+    if (!device) {
+        SSG_CK(idx->outbuf.ensure(size_t(m) * k * 8), "allocating result staging");
+        d_ids = static_cast<uint32_t *>(idx->outbuf.p);
+        d_dists = reinterpret_cast<float *>(static_cast<char *>(idx->outbuf.p) + size_t(m) * k * 4);
+    }
+    rc = run_knn(idx, dq, dqn, m, k, 0, d_ids, d_dists);
+    if (rc) return rc;
+    if (!device) {
+        SSG_CK(cudaMemcpyAsync(ids, d_ids, size_t(m) * k * 4, cudaMemcpyDeviceToHost, idx->stream), "copying ids");
+        SSG_CK(cudaMemcpyAsync(dists, d_dists, size_t(m) * k * 4, cudaMemcpyDeviceToHost, idx->stream),
+               "copying distances");
+    }
+    return finish_call(idx, !(device && (flags & 1)));
+}
+
+int allknn_common(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *ids, float *dists, bool device) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    const int64_t n = idx->n;
+    if (n <= 0) return fail(idx, SSG_EINVAL, "allknn needs a non-empty index");
+    const int64_t kmax = exclude_self ? n - 1 : n;
+    if (k <= 0 || k > kmax)
+        return fail(idx, SSG_EINVAL, "allknn needs 0 < k <= %lld (got %d)", (long long)kmax, k);
+    if (!ids || !dists) return fail(idx, SSG_EINVAL, "NULL output pointer");
+    const float *dqn = nullptr;
+    if (idx->metric == SSG_METRIC_COSINE) dqn = static_cast<const float *>(idx->db_norm.p);
+    uint32_t *d_ids = ids;
+    float *d_dists = dists;
+    if (!device) {
+        SSG_CK(idx->outbuf.ensure(size_t(n) * k * 8), "allocating result staging");
+        d_ids = static_cast<uint32_t *>(idx->outbuf.p);
+        d_dists = reinterpret_cast<float *>(static_cast<char *>(idx->outbuf.p) + size_t(n) * k * 4);
+    }
+    int rc = run_knn(idx, idx->db.p, dqn, n, k, exclude_self ? 1 : 0, d_ids, d_dists);
+    if (rc) return rc;
+    if (!device) {
+        SSG_CK(cudaMemcpyAsync(ids, d_ids, size_t(n) * k * 4, cudaMemcpyDeviceToHost, idx->stream), "copying ids");
+        SSG_CK(cudaMemcpyAsync(dists, d_dists, size_t(n) * k * 4, cudaMemcpyDeviceToHost, idx->stream),
+               "copying distances");
+    }
+    return finish_call(idx, true);
+}
+
+}  // namespace
+
+namespace ssg {
+int device_sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!cached[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 148;
+        cached[dev] = v;
+    }
+    return cached[dev];
+}
+}  // namespace ssg
+
+extern "C" {
+
+int ssg_version(void) { return 100; }
+
+int ssg_create(int metric, int elem_type, int64_t dim, int64_t n, const void *host_db, int64_t ld,
+               int precision_mode, ssg_index **out) {
+    return create_common(metric, elem_type, dim, n, host_db, ld, precision_mode, out, false);
+}
+
+int ssg_create_device(int metric, int elem_type, int64_t dim, int64_t n, const void *dev_db, int64_t ld,
+                      int precision_mode, ssg_index **out) {
+    return create_common(metric, elem_type, dim, n, dev_db, ld, precision_mode, out, true);
+}
+
+int ssg_search(ssg_index *idx, const void *host_q, int64_t dim, int64_t m, int32_t k, uint32_t *out_ids,
+               float *out_dists, int32_t flags) {
+    return search_common(idx, host_q, dim, m, k, out_ids, out_dists, flags, false);
+}
+
+int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k, uint32_t *dev_ids,
+                      float *dev_dists, int32_t flags) {
+    return search_common(idx, dev_q, idx ? idx->dim : 0, m, k, dev_ids, dev_dists, flags, true);
+}
+
+int ssg_allknn(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *out_ids, float *out_dists) {
+    return allknn_common(idx, k, exclude_self, out_ids, out_dists, false);
+}
+
+int ssg_allknn_device(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *dev_ids, float *dev_dists) {
+    return allknn_common(idx, k, exclude_self, dev_ids, dev_dists, true);
+}
+
+int ssg_append(ssg_index *idx, const void *host_rows, int64_t count) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (count < 0) return fail(idx, SSG_EINVAL, "negative count");
+    if (count == 0) return SSG_OK;
+    if (!host_rows) return fail(idx, SSG_EINVAL, "rows pointer is NULL");
+    if (idx->n + count >= (int64_t(1) << 32) - 1) return fail(idx, SSG_EINVAL, "too many objects");
+    return add_rows(idx, host_rows, count, idx->dim, false);
+}
+
+int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len, uint32_t *ids, float *dists) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (m <= 0) return fail(idx, SSG_EINVAL, "empty set of queries");
+    if (len <= 0) return fail(idx, SSG_EINVAL, "candidate lists must be non-empty");
+    if (len > 16384) return fail(idx, SSG_EUNSUPPORTED, "candidate lists longer than 16384 are not supported");
+    if (!host_q || !ids || !dists) return fail(idx, SSG_EINVAL, "NULL pointer");
+    for (int64_t i = 0; i < m * int64_t(len); ++i)
+        if (ids[i] > idx->n) return fail(idx, SSG_EINVAL, "candidate id %u out of range 1..%lld", ids[i], (long long)idx->n);
+    const void *dq;
+    const float *dqn;
+    int rc = prepare_queries(idx, host_q, m, false, &dq, &dqn);
+    if (rc) return rc;
+    SSG_CK(idx->outbuf.ensure(size_t(m) * len * 8), "allocating rerank staging");
+    uint32_t *d_ids = static_cast<uint32_t *>(idx->outbuf.p);
+    float *d_d = reinterpret_cast<float *>(static_cast<char *>(idx->outbuf.p) + size_t(m) * len * 4);
+    SSG_CK(cudaMemcpyAsync(d_ids, ids, size_t(m) * len * 4, cudaMemcpyHostToDevice, idx->stream), "copying ids");
+    SSG_CK(cudaMemcpyAsync(d_d, dists, size_t(m) * len * 4, cudaMemcpyHostToDevice, idx->stream), "copying dists");
+    SSG_CK(ssg::launch_rerank(idx->metric, idx->db.p, static_cast<const float *>(idx->db_norm.p), idx->dim, dq, dqn,
+                              m, len, d_ids, d_d, idx->stream, &idx->last_launches),
+           "launching rerank");
+    SSG_CK(cudaMemcpyAsync(ids, d_ids, size_t(m) * len * 4, cudaMemcpyDeviceToHost, idx->stream), "copying ids");
+    SSG_CK(cudaMemcpyAsync(dists, d_d, size_t(m) * len * 4, cudaMemcpyDeviceToHost, idx->stream), "copying dists");
+    return finish_call(idx, true);
+}
+
+int ssg_set_param(ssg_index *idx, const char *key, double value) {
+    if (!idx || !key) return fail(idx, SSG_EINVAL, "NULL index or key");
+    Guard g(idx, false);
+    std::string k(key);
+    if (k == "splits") {
+        if (value < 0 || value > 65535) return fail(idx, SSG_EINVAL, "splits out of range");
+        idx->splits_param = int(value);
+    } else if (k == "overfetch") {
+        if (!(value >= 1.0 && value <= 64.0)) return fail(idx, SSG_EINVAL, "overfetch must be in [1, 64]");
+        idx->overfetch = value;
+    } else if (k == "profile") {
+        idx->profile = value != 0.0;
+        if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
+    } else {
+        return fail(idx, SSG_EINVAL, "unknown parameter '%s'", key);
+    }
+    return SSG_OK;
+}
+
+int ssg_get_param(ssg_index *idx, const char *key, double *value) {
+    if (!idx || !key || !value) return fail(idx, SSG_EINVAL, "NULL argument");
+    Guard g(idx, false);
+    std::string k(key);
+    if (k == "n") *value = double(idx->n);
+    else if (k == "dim") *value = double(idx->dim);
+    else if (k == "metric") *value = idx->metric;
+    else if (k == "precision") *value = idx->prec;
+    else if (k == "splits") *value = idx->splits_param;
+    else if (k == "overfetch") *value = idx->overfetch;
+    else if (k == "profile") *value = idx->profile;
+    else if (k == "main_kernel_ms") *value = idx->main_ms;
+    else if (k == "main_kernel_launches") *value = double(idx->main_launches);
+    else if (k == "kernel_launches") *value = idx->last_launches;
+    else if (k == "device_bytes")
+        *value = double(idx->db.bytes + idx->db_norm.bytes + idx->qbuf.bytes + idx->qnorm.bytes + idx->cand.bytes +
+                        idx->gheap.bytes + idx->outbuf.bytes + idx->stage.bytes);
+    else return fail(idx, SSG_EINVAL, "unknown parameter '%s'", key);
+    return SSG_OK;
+}
+
+int ssg_set_stream(ssg_index *idx, void *stream) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (idx->own_stream && idx->stream) cudaStreamDestroy(idx->stream);
+    idx->stream = static_cast<cudaStream_t>(stream);
+    idx->own_stream = false;
+    return SSG_OK;
+}
+
+int ssg_last_error(ssg_index *idx, char *buf, int64_t len) {
+    const char *src = idx ? idx->err : g_err;
+    int full = int(strlen(src));
+    if (buf && len > 0) {
+        int64_t c = std::min<int64_t>(full, len - 1);
+        memcpy(buf, src, size_t(c));
+        buf[c] = '\0';
+    }
+    return full;
+}
+
+void ssg_destroy(ssg_index *idx) {
+    if (!idx) return;
+    cudaSetDevice(idx->device);
+    if (idx->stream) cudaStreamSynchronize(idx->stream);
+    idx->db.release();
+    idx->db_norm.release();
+    idx->qbuf.release();
+    idx->qnorm.release();
+    idx->qraw.release();
+    idx->cand.release();
+    idx->gheap.release();
+    idx->outbuf.release();
+    idx->stage.release();
+    if (idx->ev0) cudaEventDestroy(idx->ev0);
+    if (idx->ev1) cudaEventDestroy(idx->ev1);
+    if (idx->own_stream && idx->stream) cudaStreamDestroy(idx->stream);
+    delete idx;
+}
+
+}  // extern "C"

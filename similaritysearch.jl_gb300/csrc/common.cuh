@@ -1,0 +1,141 @@
+// common.cuh -- shared device helpers of libssgpu: (distance, id) keys and the
+// thread-private bounded max-heap that every scan kernel uses as its top-k.
+//
+// Ordering contract.  SimilaritySearch.jl's KnnSorted keeps results sorted by
+// distance and inserts an item AFTER existing equal distances, rejecting an
+// item equal to the frontier when full (src/pqueue/knnsorted.jl:68-101,163).
+// Because ExhaustiveSearch pushes ids in increasing order
+// (src/exact/sequential-exhaustive.jl:73-76), the result is the k smallest
+// items under the lexicographic order (distance, id).  Here that order is a
+// single 64-bit key: the float distance mapped to an order-preserving uint32
+// in the high word and the 0-based id in the low word.  Comparing keys is then
+// exactly the reference's order, including its tie rule.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ssg {
+
+constexpr uint64_t KEY_EMPTY = ~0ull;
+
+// Order-preserving float -> uint32 (for non-NaN floats).  -0.0 is first
+// folded onto +0.0, since the reference compares them as equal.
+__host__ __device__ __forceinline__ uint32_t float_to_ordered(float f) {
+    f = f + 0.0f;  // -0.0 + 0.0 == +0.0 in round-to-nearest
+    uint32_t u;
+#ifdef __CUDA_ARCH__
+    u = __float_as_uint(f);
+#else
+    __builtin_memcpy(&u, &f, 4);
+#endif
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+#ifdef __CUDA_ARCH__
+    f = __uint_as_float(b);
+#else
+    __builtin_memcpy(&f, &b, 4);
+#endif
+    return f;
+}
+
+__host__ __device__ __forceinline__ uint64_t make_key(float d, uint32_t id0) {
+    return (static_cast<uint64_t>(float_to_ordered(d)) << 32) | id0;
+}
+
+__host__ __device__ __forceinline__ float key_dist(uint64_t key) {
+    return ordered_to_float(static_cast<uint32_t>(key >> 32));
+}
+
+__host__ __device__ __forceinline__ uint32_t key_id0(uint64_t key) {
+    return static_cast<uint32_t>(key & 0xffffffffu);
+}
+
+// Thread-private max-heap of `kk` keys laid out with stride `st` (so the
+// heaps of the threads of a block interleave and a warp touching the same
+// slot hits distinct banks).  h[0] is the largest kept key == the frontier.
+struct Heap {
+    uint64_t *h;
+    int kk;
+    int st;
+
+    __device__ __forceinline__ void init() {
+        for (int i = 0; i < kk; ++i) h[i * st] = KEY_EMPTY;
+    }
+    __device__ __forceinline__ uint64_t top() const { return h[0]; }
+
+    // Replaces the top with `key` (caller checked key < top) and sifts down.
+    __device__ __forceinline__ uint64_t replace_top(uint64_t key) {
+        int i = 0;
+        while (true) {
+            int l = 2 * i + 1;
+            if (l >= kk) break;
+            int c = l;
+            uint64_t hc = h[l * st];
+            int r = l + 1;
+            if (r < kk) {
+                uint64_t hr = h[r * st];
+                if (hr > hc) { hc = hr; c = r; }
+            }
+            if (hc <= key) break;
+            h[i * st] = hc;
+            i = c;
+        }
+        h[i * st] = key;
+        return h[0];
+    }
+
+    // In-place heapsort -> ascending keys in h[0 .. kk-1].
+    __device__ void sort_ascending() {
+        for (int end = kk - 1; end > 0; --end) {
+            uint64_t top = h[0];
+            uint64_t last = h[end * st];
+            h[end * st] = top;
+            // sift `last` down from the root within [0, end)
+            int i = 0;
+            while (true) {
+                int l = 2 * i + 1;
+                if (l >= end) break;
+                int c = l;
+                uint64_t hc = h[l * st];
+                int r = l + 1;
+                if (r < end) {
+                    uint64_t hr = h[r * st];
+                    if (hr > hc) { hc = hr; c = r; }
+                }
+                if (hc <= last) break;
+                h[i * st] = hc;
+                i = c;
+            }
+            h[i * st] = last;
+        }
+    }
+};
+
+// Bitonic sort of P (a power of two) keys in shared memory by the whole block.
+__device__ __forceinline__ void block_bitonic_sort(uint64_t *s, int P) {
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < (P >> 1); i += blockDim.x) {
+                int pos = 2 * i - (i & (stride - 1));
+                int partner = pos + stride;
+                bool asc = (pos & size) == 0;
+                uint64_t a = s[pos], b = s[partner];
+                if ((a > b) == asc) { s[pos] = b; s[partner] = a; }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+inline int next_pow2(int64_t v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+}  // namespace ssg

@@ -1,0 +1,145 @@
+// hamming.cu -- binary Hamming scan with a fused bounded top-k.
+//
+// Replaces search(::ExhaustiveSearch) over MatrixDatabase{UInt64} sketches
+// with Dist.Bits.Hamming: d = Float32(sum_w popcount(x_w xor q_w))
+// (src/dist/bits.jl:18-25), pushed into KnnSorted in id order
+// (src/exact/sequential-exhaustive.jl:73-76).  Distances are integers, so the
+// (distance, id) keys -- and therefore ids, distances and their order -- are
+// bit-exact with the reference.
+//
+// Block = QPB threads, one query per thread; the query's words live in
+// registers (zero-padded to WMAX words).  Database sketches stream through
+// shared memory in tiles of TN rows and are read with 128-bit broadcast loads;
+// every thread XORs + popcounts them against its own query and pushes the
+// distance into its private max-heap when it beats the frontier.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ssg {
+
+namespace {
+
+constexpr int TN = 64;
+
+template <int WMAX, int QPB>
+__host__ __device__ constexpr size_t ham_static_smem() {
+    return size_t(TN) * WMAX * 8;
+}
+
+template <int WMAX, int QPB>
+__global__ void __launch_bounds__(QPB)
+hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__restrict__ Q,
+               int heap_in_smem) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t(*xs)[WMAX] = reinterpret_cast<uint64_t(*)[WMAX]>(smem);
+    uint64_t *hbase = heap_in_smem
+        ? reinterpret_cast<uint64_t *>(smem + ham_static_smem<WMAX, QPB>())
+        : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk) * QPB;
+
+    const int t = threadIdx.x;
+    const int W = int(a.dim);
+    const int64_t qi = int64_t(blockIdx.x) * QPB + t;
+    const bool qvalid = qi < a.m;
+    const int64_t lo = int64_t(blockIdx.y) * a.split_len;
+    const int64_t hi = lo + a.split_len < a.n ? lo + a.split_len : a.n;
+
+    uint64_t q[WMAX];
+#pragma unroll
+    for (int w = 0; w < WMAX; ++w) q[w] = (qvalid && w < W) ? Q[qi * W + w] : 0ull;
+
+    Heap H{hbase + t, a.kk, QPB};
+    H.init();
+    uint64_t top = KEY_EMPTY;
+    int topd = 0x7fffffff;
+
+    for (int64_t j0 = lo; j0 < hi; j0 += TN) {
+        __syncthreads();
+        for (int e = t; e < TN * WMAX; e += QPB) {
+            int r = e / WMAX, c = e % WMAX;
+            int64_t xr = j0 + r;
+            xs[r][c] = (xr < hi && c < W) ? db[xr * W + c] : 0ull;
+        }
+        __syncthreads();
+        if (!qvalid) continue;
+        const int jn = hi - j0 < TN ? int(hi - j0) : TN;
+        for (int j = 0; j < jn; ++j) {
+            int d = 0;
+#pragma unroll
+            for (int w = 0; w < WMAX; w += 2) {
+                const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(&xs[j][w]);
+                d += __popcll(q[w] ^ x.x) + __popcll(q[w + 1] ^ x.y);
+            }
+            if (d <= topd) {
+                const uint64_t key = make_key(float(d), uint32_t(j0 + j + a.id_base));
+                if (key < top) {
+                    top = H.replace_top(key);
+                    topd = (top == KEY_EMPTY) ? 0x7fffffff : int(key_dist(top));
+                }
+            }
+        }
+    }
+    if (qvalid) {
+        H.sort_ascending();
+        uint64_t *out = a.cand + (size_t(qi) * a.splits + blockIdx.y) * a.kk;
+        for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * QPB];
+    }
+}
+
+constexpr size_t kSmemBudget = 200 * 1024;
+
+template <int WMAX, int QPB>
+bool ham_heap_fits(int kk) {
+    return ham_static_smem<WMAX, QPB>() + size_t(kk) * QPB * 8 <= kSmemBudget;
+}
+
+template <int WMAX>
+int ham_qpb(int kk) { return ham_heap_fits<WMAX, 128>(kk) ? 128 : 32; }
+
+template <int WMAX, int QPB>
+cudaError_t launch_ham_t(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
+    const bool in_smem = ham_heap_fits<WMAX, QPB>(a.kk);
+    size_t smem = ham_static_smem<WMAX, QPB>() + (in_smem ? size_t(a.kk) * QPB * 8 : 0);
+    auto kern = hamming_kernel<WMAX, QPB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((a.m + QPB - 1) / QPB), unsigned(a.splits));
+    kern<<<grid, QPB, smem, st>>>(a, db, q, in_smem ? 1 : 0);
+    return cudaGetLastError();
+}
+
+template <int WMAX>
+cudaError_t launch_ham_w(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
+    return ham_qpb<WMAX>(a.kk) == 128 ? launch_ham_t<WMAX, 128>(a, db, q, st)
+                                      : launch_ham_t<WMAX, 32>(a, db, q, st);
+}
+
+template <int WMAX>
+size_t ham_gheap(const ScanArgs &a) {
+    int qpb = ham_qpb<WMAX>(a.kk);
+    bool fits = qpb == 128 ? ham_heap_fits<WMAX, 128>(a.kk) : ham_heap_fits<WMAX, 32>(a.kk);
+    if (fits) return 0;
+    return size_t((a.m + qpb - 1) / qpb) * a.splits * size_t(a.kk) * qpb * 8;
+}
+
+}  // namespace
+
+size_t hamming_gheap_bytes(const ScanArgs &a) {
+    if (a.dim <= 2) return ham_gheap<2>(a);
+    if (a.dim <= 4) return ham_gheap<4>(a);
+    if (a.dim <= 8) return ham_gheap<8>(a);
+    if (a.dim <= 16) return ham_gheap<16>(a);
+    return ham_gheap<32>(a);
+}
+
+cudaError_t launch_hamming(const ScanArgs &a, const uint64_t *db, const uint64_t *q,
+                           cudaStream_t st, int *launches) {
+    if (a.dim > 32) return cudaErrorInvalidValue;
+    if (launches) *launches += 1;
+    if (a.dim <= 2) return launch_ham_w<2>(a, db, q, st);
+    if (a.dim <= 4) return launch_ham_w<4>(a, db, q, st);
+    if (a.dim <= 8) return launch_ham_w<8>(a, db, q, st);
+    if (a.dim <= 16) return launch_ham_w<16>(a, db, q, st);
+    return launch_ham_w<32>(a, db, q, st);
+}
+
+}  // namespace ssg

@@ -1,0 +1,302 @@
+"""GPUExhaustiveSearch: the drop-in index for the searchbatch / allknn path.
+
+Mirrors the reference's ``AbstractSearchIndex`` surface for
+``ExhaustiveSearch`` / ``ParallelExhaustiveSearch``
+(src/exact/sequential-exhaustive.jl:18-80, src/exact/parallel-exhaustive.jl:26-123):
+``search``, ``searchbatch``, ``searchbatch_b`` (``searchbatch!``), ``allknn``,
+``allknn_b``, ``push_item_b``, ``append_items_b``, ``index_b``, ``distance``,
+``database``, ``len``.  Julia's ``f!`` is spelled ``f_b`` here.
+
+Result matrices keep Julia's shapes: ``ids`` is a ``(k, m)`` UInt32 array and
+``dists`` a ``(k, m)`` Float32 array, both Fortran-ordered so that column ``j``
+(query ``j``) is contiguous -- the bytes of a Julia ``Matrix``.  Ids are
+1-based; unfilled slots hold 0 / Inf32.
+
+Every call goes through libssgpu.so.  There is no CPU path: without the
+built library or a GPU, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .db import AbstractDatabase, MatrixDatabase, VectorDatabase, as_database
+from .dist import PreMetric
+from .log import LOG, InformativeLog
+from .pqueue import AbstractKnnQueue, KnnSorted
+
+ArgumentError = N.ArgumentError
+
+_ELEM = {
+    np.dtype(np.float32): N.ELEM_F32,
+    np.dtype(np.uint64): N.ELEM_U64,
+    np.dtype(np.float64): N.ELEM_F64,
+    np.dtype(np.float16): N.ELEM_F16,
+    np.dtype(np.uint8): N.ELEM_U8,
+    np.dtype(np.int8): N.ELEM_I8,
+}
+_PREC = {"fp32": N.PREC_FP32, "bf16": N.PREC_BF16, "fp8": N.PREC_FP8}
+
+
+class GenericContext:
+    """Mirror of GenericContext (src/SimilaritySearch.jl:192-224): logger and
+    the distance-evaluation counters (``costdists``)."""
+
+    def __init__(self, verbose: bool = True, logger=None, maxbatches: int = 64):
+        self.verbose = verbose
+        self.logger = InformativeLog() if logger is None else logger
+        self.maxbatches = maxbatches
+        self.costdists = [0] * maxbatches
+        self.costblocks = [0] * maxbatches
+        self.batchid = 0
+
+
+def add_distance_evaluations(ctx, v: int):
+    # add_distance_evaluations!(ctx, v) (SimilaritySearch.jl:224)
+    ctx.costdists[ctx.batchid] += int(v)
+
+
+def distance_evaluations(ctx) -> int:
+    return int(sum(ctx.costdists))
+
+
+def _element_type(dist: PreMetric, dtype) -> int:
+    dt = np.dtype(dtype)
+    if dist.code == N.METRIC_HAMMING:
+        if dt != np.uint64:
+            raise ArgumentError("Bits.Hamming needs UInt64 sketches")
+        return N.ELEM_U64
+    if dt == np.float32:
+        return N.ELEM_F32
+    if not dist.cast_f32:
+        raise ArgumentError(f"{dist!r} on {dt} data: use the Dist.CastF32 twin to cast to Float32")
+    if dt not in _ELEM:
+        raise ArgumentError(f"element type {dt} is not supported")
+    return _ELEM[dt]
+
+
+class GPUExhaustiveSearch:
+    """Exact brute-force index on one GPU.  ``precision`` selects the plain
+    FP32 method ("fp32") or the reduced-precision ones with FP32 rerank."""
+
+    def __init__(self, dist: PreMetric, db, precision: str = "fp32", **params):
+        self.dist = dist
+        self.db = as_database(db)
+        self.precision = precision
+        if precision not in _PREC:
+            raise ArgumentError(f"unknown precision {precision!r}")
+        rows = self.db.rows()
+        if rows.ndim != 2 or rows.shape[1] == 0:
+            raise ArgumentError("GPUExhaustiveSearch needs the database's dimension (a (dim, n) matrix)")
+        self._elem = _element_type(dist, rows.dtype)
+        self._dtype = rows.dtype
+        self.dim = rows.shape[1]
+        h = C.c_void_p()
+        lib = N.lib()
+        N.check(lib.ssg_create(dist.code, self._elem, self.dim, rows.shape[0], rows.ctypes.data_as(C.c_void_p),
+                               self.dim, _PREC[precision], C.byref(h)))
+        self._h = h
+        for k, v in params.items():
+            self.set_param(k, v)
+
+    # -- plumbing --------------------------------------------------------
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().ssg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_param(self, key: str, value: float):
+        N.check(N.lib().ssg_set_param(self._h, key.encode(), float(value)), self._h)
+
+    def get_param(self, key: str) -> float:
+        v = C.c_double()
+        N.check(N.lib().ssg_get_param(self._h, key.encode(), C.byref(v)), self._h)
+        return v.value
+
+    def __len__(self):
+        return int(self.get_param("n"))
+
+    def _queries(self, Q) -> np.ndarray:
+        Qdb = as_database(Q)
+        rows = Qdb.rows()
+        if rows.ndim != 2 or (rows.shape[0] > 0 and rows.shape[1] != self.dim):
+            raise ArgumentError(f"queries have dimension {rows.shape[-1]}, the index has {self.dim}")
+        if rows.dtype != self._dtype:
+            rows = rows.astype(self._dtype)
+        return np.ascontiguousarray(rows)
+
+
+def distance(idx: GPUExhaustiveSearch):
+    return idx.dist
+
+
+def database(idx: GPUExhaustiveSearch, i: int | None = None):
+    return idx.db if i is None else idx.db[i]
+
+
+def _check_out(ids, dists, m):
+    if ids.dtype != np.uint32 or dists.dtype != np.float32:
+        raise ArgumentError("ids must be UInt32 and dists Float32")
+    if ids.ndim != 2 or ids.shape != dists.shape:
+        raise ArgumentError("ids and dists must be (k, m) matrices of the same shape")
+    if ids.shape[1] != m:
+        raise ArgumentError("the number of queries is different from the given output containers")
+
+
+def _col_major_view(a: np.ndarray):
+    """(k, m) matrix -> (pointer, needs_copy_back) with column-contiguous bytes."""
+    if a.flags.f_contiguous:
+        return a, False
+    return np.asfortranarray(a), True
+
+
+def searchbatch_b(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, ids: np.ndarray, dists: np.ndarray,
+                  sorted: bool = False):
+    """searchbatch!(index, ctx, Q, ids, dists; sorted) -- src/SimilaritySearch.jl:331-348.
+    Columns come back sorted by (distance, id) whether or not ``sorted``."""
+    rows = idx._queries(Q)
+    m = rows.shape[0]
+    if m <= 0:
+        raise ArgumentError("empty set of queries")
+    _check_out(ids, dists, m)
+    k = ids.shape[0]
+    oi, ci = _col_major_view(ids)
+    od, cd = _col_major_view(dists)
+    N.check(N.lib().ssg_search(idx.handle, rows.ctypes.data_as(C.c_void_p), idx.dim, m, k,
+                               oi.ctypes.data_as(C.c_void_p), od.ctypes.data_as(C.c_void_p), 0), idx.handle)
+    if ci:
+        ids[...] = oi
+    if cd:
+        dists[...] = od
+    add_distance_evaluations(ctx, len(idx) * m)
+    return ids, dists
+
+
+def searchbatch(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, k: int, sorted: bool = True):
+    """searchbatch(index, ctx, Q, k) -> (ids (k, m), dists (k, m))  -- SimilaritySearch.jl:309-313"""
+    m = len(as_database(Q))
+    ids = np.zeros((k, m), dtype=np.uint32, order="F")
+    dists = np.full((k, m), np.inf, dtype=np.float32, order="F")
+    return searchbatch_b(idx, ctx, Q, ids, dists, sorted=sorted)
+
+
+def search(idx: GPUExhaustiveSearch, ctx: GenericContext, q, res: AbstractKnnQueue):
+    """search(index, ctx, q, res): one query as a batch of one; the results are
+    pushed into ``res`` in (distance, id) order (sequential-exhaustive.jl:68-80)."""
+    if not isinstance(res, KnnSorted):
+        raise ArgumentError("the GPU index fills KnnSorted queues only")
+    k = res.maxlength()
+    q = np.asarray(q)
+    Qm = MatrixDatabase(q.reshape(-1, 1))
+    ids, dists = searchbatch(idx, ctx, Qm, k)
+    for i in range(k):
+        if ids[i, 0] == 0:
+            break
+        res.push_item(int(ids[i, 0]), float(dists[i, 0]))
+    return res
+
+
+def allknn_b(idx: GPUExhaustiveSearch, ctx: GenericContext, ids: np.ndarray, dists: np.ndarray,
+             sort: bool = True, progress=None, exclude_self: bool = False):
+    """allknn!(index, ctx, ids, dists) -- src/allknn.jl:66-91.  The object
+    itself is kept unless ``exclude_self`` (an extension of this index)."""
+    n = len(idx)
+    if ids.ndim != 2 or ids.shape != dists.shape:
+        raise ArgumentError("ids and dists must be (k, n) matrices")
+    k, nn = ids.shape
+    if not n > 0:
+        raise ArgumentError("invalid assertion n > 0")
+    if nn != n:
+        raise ArgumentError("invalid assertion n == m")
+    if not 0 < k <= n:
+        raise ArgumentError("invalid assertion 0 < k <= n")
+    oi, ci = _col_major_view(ids)
+    od, cd = _col_major_view(dists)
+    N.check(N.lib().ssg_allknn(idx.handle, k, 1 if exclude_self else 0, oi.ctypes.data_as(C.c_void_p),
+                               od.ctypes.data_as(C.c_void_p)), idx.handle)
+    if ci:
+        ids[...] = oi
+    if cd:
+        dists[...] = od
+    add_distance_evaluations(ctx, n * n)
+    return ids, dists
+
+
+def allknn(idx: GPUExhaustiveSearch, ctx: GenericContext, k: int, sort: bool = True, progress=None,
+           exclude_self: bool = False):
+    """allknn(index, ctx, k) -> (ids (k, n), dists (k, n)) -- src/allknn.jl:39-47"""
+    n = len(idx)
+    ids = np.zeros((k, n), dtype=np.uint32, order="F")
+    dists = np.full((k, n), np.inf, dtype=np.float32, order="F")
+    return allknn_b(idx, ctx, ids, dists, sort=sort, progress=progress, exclude_self=exclude_self)
+
+
+def push_item_b(idx: GPUExhaustiveSearch, ctx: GenericContext, u):
+    """push_item!(index, ctx, u) -- sequential-exhaustive.jl:33-38"""
+    row = np.ascontiguousarray(np.asarray(u, dtype=idx._dtype).reshape(1, -1))
+    if row.shape[1] != idx.dim:
+        raise ArgumentError("object dimension does not match the index")
+    N.check(N.lib().ssg_append(idx.handle, row.ctypes.data_as(C.c_void_p), 1), idx.handle)
+    if isinstance(idx.db, VectorDatabase):
+        idx.db.push_item(row[0])
+    else:
+        idx.db = MatrixDatabase(np.concatenate([idx.db.matrix, row.T], axis=1))
+    n = len(idx)
+    LOG(ctx.logger, "add!", idx, ctx, n, n)
+    return idx
+
+
+def append_items_b(idx: GPUExhaustiveSearch, ctx: GenericContext, u: AbstractDatabase):
+    """append_items!(index, ctx, db) -- sequential-exhaustive.jl:40-46: one
+    ``add!`` event for the appended range (none for an empty batch)."""
+    rows = idx._queries(u)
+    sp = len(idx) + 1
+    if rows.shape[0] > 0:
+        N.check(N.lib().ssg_append(idx.handle, rows.ctypes.data_as(C.c_void_p), rows.shape[0]), idx.handle)
+        if isinstance(idx.db, VectorDatabase):
+            idx.db.append_items(list(rows))
+        else:
+            idx.db = MatrixDatabase(np.concatenate([idx.db.matrix, rows.T], axis=1))
+    ep = len(idx)
+    if ep >= sp:
+        LOG(ctx.logger, "add!", idx, ctx, sp, ep)
+    return idx
+
+
+def index_b(idx: GPUExhaustiveSearch, ctx: GenericContext):
+    """index!(index, ctx): a no-op for a brute-force index; logs ``info``
+    (sequential-exhaustive.jl:48-53)."""
+    n = len(idx)
+    LOG(ctx.logger, "info", idx, ctx, n, n)
+    return idx
+
+
+def rerank_b(idx: GPUExhaustiveSearch, queries, knns_ids: np.ndarray, knns_dists: np.ndarray):
+    """rerank!(dist, db, queries, ids, dists) -- src/rerank.jl:77-86, on the
+    GPU against the index's database and distance.  Each column is re-scored
+    exactly (the first 0 id ends it) and sorted by (distance, id)."""
+    rows = idx._queries(queries)
+    m = rows.shape[0]
+    if knns_ids.ndim != 2 or knns_ids.shape != knns_dists.shape or knns_ids.shape[1] != m:
+        raise ArgumentError("ids and dists must be (len, m) matrices with one column per query")
+    oi, ci = _col_major_view(np.ascontiguousarray(knns_ids, dtype=np.uint32) if knns_ids.dtype != np.uint32 else knns_ids)
+    od, cd = _col_major_view(knns_dists)
+    N.check(N.lib().ssg_rerank(idx.handle, rows.ctypes.data_as(C.c_void_p), m, knns_ids.shape[0],
+                               oi.ctypes.data_as(C.c_void_p), od.ctypes.data_as(C.c_void_p)), idx.handle)
+    if oi is not knns_ids:
+        knns_ids[...] = oi
+    if od is not knns_dists:
+        knns_dists[...] = od
+    return knns_ids, knns_dists
