@@ -30,5 +30,5 @@ __all__ = [
 
 def build(verbose: bool = False) -> str:
     """Compiles libssgpu.so in-tree (nvcc, sm_103a)."""
-    from .build import build as _build
+    from .builder import build as _build
     return _build(verbose=verbose)

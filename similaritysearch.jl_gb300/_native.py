@@ -1,6 +1,6 @@
 """ctypes binding of libssgpu.so (the C ABI in include/ssgpu.h).
 
-The library is built in-tree by ``build.py``; importing this module never
+The library is built in-tree by ``builder.py``; importing this module never
 builds it.  If the shared object is missing the first call raises
 ``NativeLibraryMissing`` -- there is no CPU fallback.
 """
@@ -75,7 +75,7 @@ def lib():
         if _lib is None:
             if not os.path.exists(LIB_PATH):
                 raise NativeLibraryMissing(
-                    f"{LIB_PATH} is not built; run similaritysearch.jl_gb300/build.py (or "
+                    f"{LIB_PATH} is not built; run similaritysearch.jl_gb300/builder.py (or "
                     "__graft_entry__.build()) first")
             L = C.CDLL(LIB_PATH)
             for name, (args, res) in SIGNATURES.items():

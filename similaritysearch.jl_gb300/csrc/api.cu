@@ -19,6 +19,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -44,6 +45,7 @@ struct DevBuf {
 };
 
 bool is_float_metric(int m) { return m >= SSG_METRIC_SQL2 && m <= SSG_METRIC_IP; }
+bool is_sq_metric(int metric) { return metric == SSG_METRIC_SQL2 || metric == SSG_METRIC_L2; }
 
 size_t elem_size(int e) {
     switch (e) {
@@ -66,6 +68,16 @@ struct ssg_index {
     DevBuf db;       // n x dim Float32 rows, or n x W UInt64 sketches
     DevBuf db_norm;  // |x| per row (COSINE)
     DevBuf qbuf, qnorm, qraw, cand, gheap, outbuf, stage;
+    // BF16 tensor-core mode: operand tiles of the database and the queries,
+    // per-row norms of the padded database, and the device status word.
+    DevBuf tc_db, tc_norm, tc_q, status;
+    // plain FP32 GEMM-form path: |x|^2 per row and its maximum, query flags of
+    // the completeness check and the fallback's buffers
+    DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand;
+    float max_x_sq = 0.0f;
+    int margin_param = 0;
+    int exact_scan_param = 0;
+    int last_fallbacks = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::mutex mu;
@@ -169,6 +181,24 @@ int ensure_db_capacity(ssg_index *idx, int64_t rows) {
     return SSG_OK;
 }
 
+// (Re)builds the BF16 operand tiles and row norms of the whole database.
+// Tiles are allocated in pairs so a CTA holding two query tiles never reads
+// past the end when the database doubles as the query set (allknn).
+int build_tc_tiles(ssg_index *idx) {
+    const int64_t tiles = (ssg::tc_tiles(idx->n) + 1) / 2 * 2;
+    const size_t tb = ssg::tc_tile_bytes(idx->dim);
+    SSG_CK(idx->tc_db.ensure(size_t(tiles) * tb), "allocating BF16 database tiles");
+    SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(idx->db.p), idx->n, idx->dim, tiles,
+                                  static_cast<uint8_t *>(idx->tc_db.p), idx->stream, &idx->last_launches),
+           "building BF16 database tiles");
+    SSG_CK(idx->tc_norm.ensure(size_t(tiles) * 128 * 4), "allocating BF16 row norms");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, static_cast<const float *>(idx->db.p), idx->n, idx->dim, tiles * 128,
+                                static_cast<float *>(idx->tc_norm.p), idx->stream, &idx->last_launches),
+           "computing BF16 row norms");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building BF16 tiles");
+    return SSG_OK;
+}
+
 int add_rows(ssg_index *idx, const void *src, int64_t rows, int64_t ld, bool src_device) {
     int rc = ensure_db_capacity(idx, idx->n + rows);
     if (rc) return rc;
@@ -184,6 +214,23 @@ int add_rows(ssg_index *idx, const void *src, int64_t rows, int64_t ld, bool src
     }
     SSG_CK(cudaStreamSynchronize(idx->stream), "uploading the database");
     idx->n += rows;
+    if (is_sq_metric(idx->metric) && idx->n > 0) {
+        // |x|^2 per row (GEMM-form SqL2) and its maximum (completeness bound)
+        SSG_CK(idx->sq_norm.ensure(size_t(idx->n) * 4), "allocating squared norms");
+        SSG_CK(idx->sq_max.ensure(16), "allocating the norm maximum");
+        SSG_CK(cudaMemsetAsync(idx->sq_max.p, 0, 4, idx->stream), "clearing the norm maximum");
+        SSG_CK(ssg::launch_row_sq_norms(static_cast<const float *>(idx->db.p), idx->n, idx->dim,
+                                        static_cast<float *>(idx->sq_norm.p), static_cast<float *>(idx->sq_max.p),
+                                        idx->stream, &idx->last_launches),
+               "computing squared norms");
+        SSG_CK(cudaMemcpyAsync(&idx->max_x_sq, idx->sq_max.p, 4, cudaMemcpyDeviceToHost, idx->stream),
+               "reading the norm maximum");
+        SSG_CK(cudaStreamSynchronize(idx->stream), "computing squared norms");
+    }
+    if (idx->prec == SSG_PREC_BF16) {
+        rc = build_tc_tiles(idx);
+        if (rc) return rc;
+    }
     return SSG_OK;
 }
 
@@ -202,8 +249,13 @@ int validate_create(int metric, int elem, int64_t dim, int64_t n, int64_t ld, in
     if (n < 0 || n >= (int64_t(1) << 32) - 1)
         return fail(nullptr, SSG_EINVAL, "database length %lld out of range", (long long)n);
     if (ld < dim) return fail(nullptr, SSG_EINVAL, "leading dimension %lld < dim %lld", (long long)ld, (long long)dim);
-    if (prec != SSG_PREC_FP32)
+    if (prec != SSG_PREC_FP32 && prec != SSG_PREC_BF16)
         return fail(nullptr, SSG_EUNSUPPORTED, "precision mode %d is not available in this build", prec);
+    if (prec != SSG_PREC_FP32 && metric == SSG_METRIC_HAMMING)
+        return fail(nullptr, SSG_EUNSUPPORTED, "Hamming distances are integers: only the exact mode exists");
+    if (prec == SSG_PREC_BF16 && ssg::tc_padded_k(dim) > 256)
+        return fail(nullptr, SSG_EUNSUPPORTED, "the BF16 mode keeps query tiles on chip: dim <= 256 (got %lld)",
+                    (long long)dim);
     return SSG_OK;
 }
 
@@ -253,21 +305,53 @@ int choose_splits(ssg_index *idx, int64_t m, int kk, int qpb) {
     return int(std::max<int64_t>(1, s));
 }
 
-// The search pipeline: scan (fused distances + top-k per split) then merge
-// and decode.  dq are device query rows (Float32 or UInt64), dqn their norms.
-int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
-            uint32_t *d_ids, float *d_dists) {
+// Records the scan kernel's duration when profiling (events around it on the
+// index's stream).
+struct ScanTimer {
+    ssg_index *idx;
+    explicit ScanTimer(ssg_index *i) : idx(i) {}
+    int begin() {
+        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
+        return SSG_OK;
+    }
+    int end() {
+        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
+        return SSG_OK;
+    }
+    int collect() {
+        if (!idx->profile) return SSG_OK;
+        SSG_CK(cudaEventSynchronize(idx->ev1), "timing the scan kernel");
+        float ms = 0.f;
+        SSG_CK(cudaEventElapsedTime(&ms, idx->ev0, idx->ev1), "timing the scan kernel");
+        idx->main_ms += ms;
+        idx->main_launches += 1;
+        return SSG_OK;
+    }
+};
+
+#define SSG_RC(call)        \
+    do {                    \
+        int _rc = (call);   \
+        if (_rc) return _rc; \
+    } while (0)
+
+// The exact scan (direct FP32 or Hamming) then merge and decode.  dq are
+// device query rows (Float32 or UInt64), dqn their norms (Cosine).  self_ids
+// (device, optional) names each query's own object for exclude_self when the
+// queries are not the contiguous range 0..m-1 of the database.
+int run_exact_scan(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                   const int64_t *self_ids, uint32_t *d_ids, float *d_dists, DevBuf &cand) {
     const int take = k + (exclude_self ? 1 : 0);
     const int kk = int(std::min<int64_t>(take, std::max<int64_t>(1, idx->n)));
-    const int qpb = (idx->metric == SSG_METRIC_HAMMING) ? 128 : 128;
-    const int splits = choose_splits(idx, m, kk, qpb);
+    const int splits = choose_splits(idx, m, kk, 128);
     const int64_t split_len = (idx->n + splits - 1) / splits;
     // bound the candidate scratch to ~1 GiB by processing queries in chunks
     const size_t per_query = size_t(splits) * kk * 8;
     int64_t chunk = std::max<int64_t>(1, int64_t((size_t(1) << 30) / per_query));
     chunk = std::min<int64_t>(chunk, m);
-    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    SSG_CK(cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
     const size_t qrow_bytes = size_t(idx->dim) * (idx->metric == SSG_METRIC_HAMMING ? 8 : 4);
+    ScanTimer timer(idx);
     for (int64_t c0 = 0; c0 < m; c0 += chunk) {
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
         ssg::ScanArgs a{};
@@ -278,7 +362,7 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
         a.kk = kk;
         a.splits = splits;
         a.split_len = split_len;
-        a.cand = static_cast<uint64_t *>(idx->cand.p);
+        a.cand = static_cast<uint64_t *>(cand.p);
         a.id_base = 0;
         const void *qc = static_cast<const char *>(dq) + size_t(c0) * qrow_bytes;
         size_t gh = idx->metric == SSG_METRIC_HAMMING ? ssg::hamming_gheap_bytes(a) : ssg::direct_gheap_bytes(a);
@@ -286,7 +370,7 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
             SSG_CK(idx->gheap.ensure(gh), "allocating heap scratch");
             a.gheap = static_cast<uint64_t *>(idx->gheap.p);
         }
-        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
+        SSG_RC(timer.begin());
         cudaError_t e;
         if (idx->metric == SSG_METRIC_HAMMING) {
             e = ssg::launch_hamming(a, static_cast<const uint64_t *>(idx->db.p), static_cast<const uint64_t *>(qc),
@@ -297,9 +381,7 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
                                        dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches);
         }
         SSG_CK(e, "launching the scan kernel");
-        if (idx->profile) {
-            SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
-        }
+        SSG_RC(timer.end());
         ssg::FinalizeArgs f{};
         f.cand = a.cand;
         f.segs = splits;
@@ -308,9 +390,214 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
         f.k_out = k;
         f.exclude_self = exclude_self;
         f.self_base = c0;
+        f.self_ids = self_ids ? self_ids + c0 : nullptr;
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
         SSG_CK(ssg::launch_finalize(f, idx->stream, &idx->last_launches), "launching the merge kernel");
+        SSG_RC(timer.collect());
+    }
+    return SSG_OK;
+}
+
+// Candidates kept by the GEMM-form scan for SqL2 / L2 beyond the k needed.
+int gemm_margin(const ssg_index *idx, int take) {
+    return idx->margin_param > 0 ? idx->margin_param : std::max(8, (take + 3) / 4);
+}
+
+// The plain FP32 method through the register-tiled GEMM-form scan.  Dot
+// metrics get exact keys directly; SqL2 / L2 re-score kk = k + margin
+// candidates exactly, and queries whose margin is not provably enough are
+// recomputed with the exact direct scan.
+int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k, int exclude_self,
+             uint32_t *d_ids, float *d_dists, int kk) {
+    const int take = k + (exclude_self ? 1 : 0);
+    const bool sq = is_sq_metric(idx->metric);
+    const int64_t qtiles = (m + 127) / 128;
+    int64_t splits = idx->splits_param > 0 ? idx->splits_param
+                                           : (ssg::device_sm_count() + qtiles - 1) / qtiles;
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, idx->n / 512));
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / kk));
+    splits = std::max<int64_t>(1, splits);
+    const int64_t split_len = (idx->n + splits - 1) / splits;
+    const int segs = int(splits) * 2;
+    const size_t per_query = size_t(segs) * kk * 8;
+    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
+    chunk = std::min<int64_t>(chunk, m);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    if (sq) {
+        SSG_CK(idx->flags.ensure(size_t(m) * 4 + 16), "allocating query flags");
+        SSG_CK(idx->qsq.ensure(size_t(chunk) * 4 + 16), "allocating query norms");
+        SSG_CK(cudaMemsetAsync(idx->flags.p, 0, size_t(m) * 4 + 16, idx->stream), "clearing query flags");
+    }
+    int *flags = static_cast<int *>(idx->flags.p);
+    int *flag_count = flags ? flags + m : nullptr;
+    ScanTimer timer(idx);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        ssg::ScanArgs a{};
+        a.metric = idx->metric;
+        a.n = idx->n;
+        a.dim = idx->dim;
+        a.m = mc;
+        a.kk = kk;
+        a.splits = int(splits);
+        a.split_len = split_len;
+        a.cand = static_cast<uint64_t *>(idx->cand.p);
+        const float *qc = dq + size_t(c0) * idx->dim;
+        const float *xaux = sq ? static_cast<const float *>(idx->sq_norm.p) : static_cast<const float *>(idx->db_norm.p);
+        SSG_RC(timer.begin());
+        SSG_CK(ssg::launch_gemm_f32(a, static_cast<const float *>(idx->db.p), xaux, qc, dqn ? dqn + c0 : nullptr,
+                                    idx->stream, &idx->last_launches),
+               "launching the FP32 scan kernel");
+        SSG_RC(timer.end());
+        ssg::FinalizeArgs f{};
+        f.cand = a.cand;
+        f.segs = segs;
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        if (sq) {
+            float *qsq = static_cast<float *>(idx->qsq.p);
+            SSG_CK(ssg::launch_row_sq_norms(qc, mc, idx->dim, qsq, qsq + chunk, idx->stream, &idx->last_launches),
+                   "computing query norms");
+            f.check = 1;
+            f.q_sq = qsq;
+            f.max_x_sq = idx->max_x_sq;
+            f.err_scale = 4.0f * float(idx->dim + 2) * 5.9604645e-8f;
+            f.n_total = idx->n;
+            f.flags = flags + c0;
+            f.flag_count = flag_count;
+            SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                               static_cast<const float *>(idx->db_norm.p), idx->dim, qc,
+                                               nullptr, idx->stream, &idx->last_launches),
+                   "launching the rerank kernel");
+        } else {
+            SSG_CK(ssg::launch_finalize(f, idx->stream, &idx->last_launches), "launching the merge kernel");
+        }
+        SSG_RC(timer.collect());
+    }
+    if (!sq) return SSG_OK;
+    // queries whose candidate margin was not provably sufficient
+    int nflag = 0;
+    SSG_CK(cudaMemcpyAsync(&nflag, flag_count, sizeof(int), cudaMemcpyDeviceToHost, idx->stream), "reading flags");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the FP32 scan");
+    idx->last_fallbacks = nflag;
+    if (nflag == 0) return SSG_OK;
+    std::vector<int> hflags(static_cast<size_t>(m), 0);
+    SSG_CK(cudaMemcpy(hflags.data(), flags, size_t(m) * 4, cudaMemcpyDeviceToHost), "reading flags");
+    std::vector<int64_t> list;
+    list.reserve(size_t(nflag));
+    for (int64_t j = 0; j < m; ++j)
+        if (hflags[size_t(j)]) list.push_back(j);
+    const int64_t cnt = int64_t(list.size());
+    const size_t row_bytes = size_t(idx->dim) * 4;
+    SSG_CK(idx->fb_list.ensure(size_t(cnt) * 8), "allocating fallback list");
+    SSG_CK(idx->fb_q.ensure(size_t(cnt) * row_bytes), "allocating fallback queries");
+    SSG_CK(idx->fb_out.ensure(size_t(cnt) * k * 8), "allocating fallback results");
+    int64_t *dlist = static_cast<int64_t *>(idx->fb_list.p);
+    SSG_CK(cudaMemcpyAsync(dlist, list.data(), size_t(cnt) * 8, cudaMemcpyHostToDevice, idx->stream),
+           "copying fallback list");
+    SSG_CK(ssg::launch_gather_rows(dq, dlist, cnt, row_bytes, idx->fb_q.p, idx->stream, &idx->last_launches),
+           "gathering fallback queries");
+    uint32_t *fi = static_cast<uint32_t *>(idx->fb_out.p);
+    float *fd = reinterpret_cast<float *>(fi + size_t(cnt) * k);
+    SSG_RC(run_exact_scan(idx, idx->fb_q.p, nullptr, cnt, k, exclude_self, dlist, fi, fd, idx->fb_cand));
+    SSG_CK(ssg::launch_scatter_results(fi, fd, dlist, cnt, k, d_ids, d_dists, idx->stream, &idx->last_launches),
+           "scattering fallback results");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the fallback scan");
+    return SSG_OK;
+}
+
+int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+               uint32_t *d_ids, float *d_dists, bool queries_are_db);
+
+// Dispatch: BF16 tensor-core mode, Hamming, or the plain FP32 method (GEMM
+// form when its heaps fit, otherwise the exact direct scan).
+int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+            uint32_t *d_ids, float *d_dists, bool queries_are_db = false) {
+    if (idx->prec == SSG_PREC_BF16)
+        return run_knn_tc(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
+    idx->last_fallbacks = 0;
+    if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
+        const int take = k + (exclude_self ? 1 : 0);
+        int64_t kk = is_sq_metric(idx->metric) ? int64_t(take) + gemm_margin(idx, take) : take;
+        kk = std::min<int64_t>(kk, std::max<int64_t>(1, idx->n));
+        if (ssg::gemm_fits(int(kk)))
+            return run_gemm(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists, int(kk));
+    }
+    return run_exact_scan(idx, dq, dqn, m, k, exclude_self, nullptr, d_ids, d_dists, idx->cand);
+}
+
+// The BF16 pipeline: operand tiles of the queries (or the database itself for
+// allknn), the tcgen05 scan keeping kk = overfetch * k approximate candidates
+// per query and split, then the exact FP32 rerank + (distance, id) merge.
+int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+               uint32_t *d_ids, float *d_dists, bool queries_are_db) {
+    const int take = k + (exclude_self ? 1 : 0);
+    int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
+    kk64 = std::max<int64_t>(kk64, take);
+    kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
+    const int kk = int(kk64);
+    const int kp = ssg::tc_padded_k(idx->dim);
+    int qt = 0, stages = 0;
+    if (!ssg::tc_choose(kp, kk, &qt, &stages))
+        return fail(idx, SSG_EUNSUPPORTED, "overfetch x k = %d candidates do not fit the BF16 kernel", kk);
+    const int64_t qrows = int64_t(qt) * 128;
+    const int64_t qctas = (m + qrows - 1) / qrows;
+    const int64_t n_tiles = ssg::tc_tiles(idx->n);
+    int64_t splits = idx->splits_param > 0 ? idx->splits_param
+                                           : (ssg::device_sm_count() + qctas - 1) / qctas;
+    splits = std::min<int64_t>(splits, n_tiles);
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 8192 / kk));
+    splits = std::max<int64_t>(1, splits);
+    // chunk the queries (a multiple of the CTA's query rows) to bound scratch
+    const size_t per_query = size_t(splits) * kk * 8;
+    int64_t chunk = std::max<int64_t>(qrows, int64_t((size_t(1) << 30) / per_query) / qrows * qrows);
+    chunk = std::min<int64_t>(chunk, (m + qrows - 1) / qrows * qrows);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    const size_t tb = ssg::tc_tile_bytes(idx->dim);
+    const uint8_t *qtiles = static_cast<const uint8_t *>(idx->tc_db.p);
+    if (!queries_are_db) {
+        const int64_t qt_alloc = (m + qrows - 1) / qrows * qt;
+        SSG_CK(idx->tc_q.ensure(size_t(qt_alloc) * tb), "allocating BF16 query tiles");
+        SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(dq), m, idx->dim, qt_alloc,
+                                      static_cast<uint8_t *>(idx->tc_q.p), idx->stream, &idx->last_launches),
+               "building BF16 query tiles");
+        qtiles = static_cast<const uint8_t *>(idx->tc_q.p);
+    }
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
+        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb,
+                                   static_cast<const uint8_t *>(idx->tc_db.p),
+                                   static_cast<const float *>(idx->tc_norm.p), idx->n, mc, idx->dim, kk, int(splits),
+                                   static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
+                                   idx->stream, &idx->last_launches, nullptr),
+               "launching the BF16 scan kernel");
+        if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
+        ssg::FinalizeArgs f{};
+        f.cand = static_cast<const uint64_t *>(idx->cand.p);
+        f.segs = int(splits);
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        const size_t qrow_bytes = size_t(idx->dim) * 4;
+        SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim,
+                                           reinterpret_cast<const float *>(static_cast<const char *>(dq) +
+                                                                           size_t(c0) * qrow_bytes),
+                                           dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches),
+               "launching the rerank kernel");
         if (idx->profile) {
             SSG_CK(cudaEventSynchronize(idx->ev1), "timing the scan kernel");
             float ms = 0.f;
@@ -319,6 +606,12 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
             idx->main_launches += 1;
         }
     }
+    int status = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the BF16 search");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the BF16 scan kernel gave up (code %d)", status);
     return SSG_OK;
 }
 
@@ -418,7 +711,7 @@ int allknn_common(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *ids
         d_ids = static_cast<uint32_t *>(idx->outbuf.p);
         d_dists = reinterpret_cast<float *>(static_cast<char *>(idx->outbuf.p) + size_t(n) * k * 4);
     }
-    int rc = run_knn(idx, idx->db.p, dqn, n, k, exclude_self ? 1 : 0, d_ids, d_dists);
+    int rc = run_knn(idx, idx->db.p, dqn, n, k, exclude_self ? 1 : 0, d_ids, d_dists, true);
     if (rc) return rc;
     if (!device) {
         SSG_CK(cudaMemcpyAsync(ids, d_ids, size_t(n) * k * 4, cudaMemcpyDeviceToHost, idx->stream), "copying ids");
@@ -523,6 +816,11 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
     } else if (k == "overfetch") {
         if (!(value >= 1.0 && value <= 64.0)) return fail(idx, SSG_EINVAL, "overfetch must be in [1, 64]");
         idx->overfetch = value;
+    } else if (k == "margin") {
+        if (value < 0 || value > 4096) return fail(idx, SSG_EINVAL, "margin out of range");
+        idx->margin_param = int(value);
+    } else if (k == "exact_scan") {
+        idx->exact_scan_param = value != 0.0;
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -546,9 +844,14 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "main_kernel_ms") *value = idx->main_ms;
     else if (k == "main_kernel_launches") *value = double(idx->main_launches);
     else if (k == "kernel_launches") *value = idx->last_launches;
+    else if (k == "margin") *value = idx->margin_param;
+    else if (k == "exact_scan") *value = idx->exact_scan_param;
+    else if (k == "fallbacks") *value = idx->last_fallbacks;
+    else if (k == "max_x_sq") *value = idx->max_x_sq;
     else if (k == "device_bytes")
         *value = double(idx->db.bytes + idx->db_norm.bytes + idx->qbuf.bytes + idx->qnorm.bytes + idx->cand.bytes +
-                        idx->gheap.bytes + idx->outbuf.bytes + idx->stage.bytes);
+                        idx->gheap.bytes + idx->outbuf.bytes + idx->stage.bytes + idx->tc_db.bytes +
+                        idx->tc_norm.bytes + idx->tc_q.bytes);
     else return fail(idx, SSG_EINVAL, "unknown parameter '%s'", key);
     return SSG_OK;
 }
@@ -586,6 +889,13 @@ void ssg_destroy(ssg_index *idx) {
     idx->gheap.release();
     idx->outbuf.release();
     idx->stage.release();
+    idx->tc_db.release();
+    idx->tc_norm.release();
+    idx->tc_q.release();
+    idx->status.release();
+    for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
+                      &idx->fb_cand})
+        b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);
     if (idx->own_stream && idx->stream) cudaStreamDestroy(idx->stream);

@@ -17,6 +17,7 @@
 #include "kernels.h"
 
 #include <cuda_fp16.h>
+#include <algorithm>
 #include <cmath>
 
 namespace ssg {
@@ -203,7 +204,7 @@ __global__ void finalize_kernel(FinalizeArgs a, int P) {
         uint32_t *oi = a.out_ids + size_t(j) * a.k_out;
         float *od = a.out_dists + size_t(j) * a.k_out;
         int w = 0;
-        const uint32_t self0 = uint32_t(j + a.self_base);
+        const uint32_t self0 = uint32_t(a.self_ids ? a.self_ids[j] : j + a.self_base);
         bool dropped = !a.exclude_self;
         const int limit = a.k_out + (a.exclude_self ? 1 : 0);
         for (int i = 0; i < limit && i < P && w < a.k_out; ++i) {
@@ -258,7 +259,71 @@ __global__ void cast_kernel(const T *__restrict__ src, int64_t count, float *__r
     for (; i < count; i += stride) dst[i] = to_f32<T>(src[i]);
 }
 
+__global__ void row_sq_norms_kernel(const float *__restrict__ x, int64_t rows, int64_t dim,
+                                    float *__restrict__ out, float *__restrict__ max_out) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    float s = 0.0f;
+    if (i < rows) {
+        const float *r = x + i * dim;
+        for (int64_t c = 0; c < dim; ++c) s = fmaf(r[c], r[c], s);
+        out[i] = s;
+    }
+    // block max, then one atomic per block (non-negative floats order as ints)
+    for (int o = 16; o > 0; o >>= 1) s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int *>(max_out), __float_as_int(s));
+}
+
+__global__ void gather_rows_kernel(const uint32_t *__restrict__ src, const int64_t *__restrict__ idx,
+                                   int64_t count, int64_t words, uint32_t *__restrict__ dst) {
+    const int64_t total = count * words;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t r = i / words, w = i % words;
+        dst[i] = src[idx[r] * words + w];
+    }
+}
+
+__global__ void scatter_results_kernel(const uint32_t *__restrict__ si, const float *__restrict__ sd,
+                                       const int64_t *__restrict__ idx, int64_t count, int k,
+                                       uint32_t *__restrict__ ids, float *__restrict__ dists) {
+    const int64_t total = count * k;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t r = i / k, c = i % k;
+        ids[idx[r] * k + c] = si[i];
+        dists[idx[r] * k + c] = sd[i];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_row_sq_norms(const float *x, int64_t rows, int64_t dim, float *out, float *max_out,
+                                cudaStream_t st, int *launches) {
+    if (rows <= 0) return cudaSuccess;
+    if (launches) *launches += 1;
+    row_sq_norms_kernel<<<unsigned((rows + 255) / 256), 256, 0, st>>>(x, rows, dim, out, max_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const void *src, const int64_t *idx, int64_t count, size_t row_bytes, void *dst,
+                               cudaStream_t st, int *launches) {
+    if (count <= 0) return cudaSuccess;
+    const int64_t words = int64_t(row_bytes / 4);
+    int64_t blocks = std::min<int64_t>((count * words + 255) / 256, 148 * 32);
+    if (launches) *launches += 1;
+    gather_rows_kernel<<<unsigned(blocks), 256, 0, st>>>(static_cast<const uint32_t *>(src), idx, count, words,
+                                                         static_cast<uint32_t *>(dst));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, const int64_t *idx, int64_t count,
+                                   int k, uint32_t *ids, float *dists, cudaStream_t st, int *launches) {
+    if (count <= 0) return cudaSuccess;
+    int64_t blocks = std::min<int64_t>((count * k + 255) / 256, 148 * 32);
+    if (launches) *launches += 1;
+    scatter_results_kernel<<<unsigned(blocks), 256, 0, st>>>(src_ids, src_d, idx, count, k, ids, dists);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_row_norms(const float *x, int64_t rows, int64_t dim, float *out,
                              cudaStream_t st, int *launches) {

@@ -50,6 +50,18 @@ struct FinalizeArgs {
     int64_t self_base;
     uint32_t *out_ids;
     float *out_dists;
+    // optional: per-query object ids for exclude_self (overrides self_base)
+    const int64_t *self_ids = nullptr;
+    // optional completeness check of a GEMM-form candidate list (SqL2 / L2):
+    // flags[j] = 1 (and *flag_count += 1) when the kk approximate candidates
+    // do not provably contain the exact top (k + exclude_self).
+    int check = 0;
+    const float *q_sq = nullptr;   // |q|^2 per query
+    float max_x_sq = 0.0f;         // max |x|^2 over the database
+    float err_scale = 0.0f;        // c * d * 2^-24 (see finalize_rerank_kernel)
+    int64_t n_total = 0;           // database rows
+    int *flags = nullptr;
+    int *flag_count = nullptr;
 };
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t st, int *launches);
 
@@ -68,6 +80,47 @@ cudaError_t launch_cast_f32(const void *src, int elem, int64_t count, float *dst
 cudaError_t launch_rerank(int metric, const void *db, const float *db_norm, int64_t dim,
                           const void *q, const float *q_norm, int64_t m, int len,
                           uint32_t *ids, float *dists, cudaStream_t st, int *launches);
+
+// ---- BF16 tensor-core path (tc_bf16.cu) ----
+// Queries / database rows as BF16 tiles of 128 rows in the swizzled tcgen05
+// operand layout (K padded to a multiple of 32).
+int tc_padded_k(int64_t dim);
+int64_t tc_tiles(int64_t rows);
+size_t tc_tile_bytes(int64_t dim);
+// Chooses query tiles per CTA and pipeline depth; false if kk cannot fit.
+bool tc_choose(int kp, int kk, int *qt, int *stages);
+cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
+                              cudaStream_t st, int *launches);
+// |x|^2 (SqL2/L2) or 1/|x| (Cosine) per padded row.
+cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,
+                            cudaStream_t st, int *launches);
+// The fused scan: per (query, split) the kk best approximate keys.  *err is
+// set non-zero if a bounded wait gave up.
+cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                           int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
+                           cudaStream_t st, int *launches, int *qt_out);
+// Merge + exact FP32 rerank of the candidates + (distance, id) sort + decode.
+cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const float *db, const float *db_norm,
+                                   int64_t dim, const float *q, const float *q_norm, cudaStream_t st,
+                                   int *launches);
+
+// ---- plain FP32 GEMM-form scan (gemm_f32.cu) ----
+// Writes splits x 2 sorted segments of kk keys per query.
+bool gemm_fits(int kk);
+cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
+                            const float *q_norm, cudaStream_t st, int *launches);
+
+// ---- helpers (direct.cu) ----
+// out[i] = sum x^2 per row (sequential FMA) and *max_out = max over rows
+// (max_out must be zeroed first).
+cudaError_t launch_row_sq_norms(const float *x, int64_t rows, int64_t dim, float *out, float *max_out,
+                                cudaStream_t st, int *launches);
+// dst row i = src row idx[i] (rows of row_bytes bytes, a multiple of 4).
+cudaError_t launch_gather_rows(const void *src, const int64_t *idx, int64_t count, size_t row_bytes, void *dst,
+                               cudaStream_t st, int *launches);
+// ids/dists row idx[i] (k entries) = src row i.
+cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, const int64_t *idx, int64_t count,
+                                   int k, uint32_t *ids, float *dists, cudaStream_t st, int *launches);
 
 int device_sm_count();
 

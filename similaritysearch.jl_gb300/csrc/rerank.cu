@@ -6,36 +6,12 @@
 // distances to Base.sort; here ties are ordered by id, which is one of the
 // orders the reference can produce and makes the output deterministic.
 #include "common.cuh"
+#include "exact.cuh"
 #include "kernels.h"
 
 namespace ssg {
 
 namespace {
-
-// Exact distance of one (row, query) pair, summed in index order with one FMA
-// per element -- the same chain as the scan kernels and the oracle.
-template <int METRIC>
-__device__ float exact_pair(const void *dbv, int64_t row, int64_t dim, const void *qv, int64_t j,
-                            const float *xn, const float *qn) {
-    if (METRIC == HAMMING) {
-        const uint64_t *x = static_cast<const uint64_t *>(dbv) + row * dim;
-        const uint64_t *q = static_cast<const uint64_t *>(qv) + j * dim;
-        int d = 0;
-        for (int64_t w = 0; w < dim; ++w) d += __popcll(x[w] ^ q[w]);
-        return float(d);
-    }
-    const float *x = static_cast<const float *>(dbv) + row * dim;
-    const float *q = static_cast<const float *>(qv) + j * dim;
-    float acc = 0.0f;
-    if (METRIC == SQL2 || METRIC == L2) {
-        for (int64_t c = 0; c < dim; ++c) { float m = x[c] - q[c]; acc = fmaf(m, m, acc); }
-        return METRIC == L2 ? sqrtf(acc) : acc;
-    }
-    for (int64_t c = 0; c < dim; ++c) acc = fmaf(x[c], q[c], acc);
-    if (METRIC == NORMCOSINE) return 1.0f - acc;
-    if (METRIC == IP) return -acc;
-    return 1.0f - acc / (xn[row] * qn[j]);
-}
 
 template <int METRIC>
 __global__ void rerank_kernel(const void *db, const float *xn, int64_t dim, const void *q,
@@ -98,6 +74,108 @@ cudaError_t launch_rerank(int metric, const void *db, const float *db_norm, int6
         default: return cudaErrorInvalidValue;
     }
 #undef SSG_RR
+}
+
+// ---------------------------------------------------------------------------
+// Merge the per-split approximate candidates, re-rank them with the exact
+// FP32 distance and write the k best in (distance, id) order.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int METRIC>
+__global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const float *db_norm, int64_t dim,
+                                       const float *q, const float *q_norm, int P1, int P2) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *s1 = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *s2 = s1 + P1;
+    const int64_t j = blockIdx.x;
+    const int total = f.segs * f.kk;
+    const uint64_t *src = f.cand + size_t(j) * total;
+    for (int i = threadIdx.x; i < P1; i += blockDim.x) s1[i] = i < total ? src[i] : KEY_EMPTY;
+    if (f.segs > 1) block_bitonic_sort(s1, P1);
+    else __syncthreads();
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+        uint64_t key = KEY_EMPTY;
+        if (i < f.kk) {
+            const uint64_t ak = s1[i];
+            if (ak != KEY_EMPTY) {
+                const uint32_t id0 = key_id0(ak);
+                const float d = exact_pair<METRIC>(db, int64_t(id0), dim, q, j, db_norm, q_norm);
+                key = make_key(d, id0);
+            }
+        }
+        s2[i] = key;
+    }
+    if (f.check && threadIdx.x == 0) {
+        // Completeness of a GEMM-form candidate list.  With a = |x|^2 - 2 x.q
+        // the approximate value and D the exact difference-form distance,
+        // |a + |q|^2 - D| <= E = err_scale * (sqrt(max|x|^2) + |q|)^2.  Every
+        // item of the exact top `take` then has a <= a_take + 2E, so if the
+        // last kept candidate has a_last > a_take + 2E (+ the sqrt-collision
+        // allowance of L2), nothing outside the list can belong to it.
+        const int take = f.k_out + (f.exclude_self ? 1 : 0);
+        int nv = 0;
+        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
+        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
+            const float qs = f.q_sq[j];
+            const float r = sqrtf(f.max_x_sq) + sqrtf(qs);
+            const float E = f.err_scale * r * r;
+            const float a_take = key_dist(s1[take - 1]);
+            const float a_last = key_dist(s1[f.kk - 1]);
+            float slack = 2.0f * E;
+            if (METRIC == L2) slack += 8.0f * 5.96e-8f * fabsf(a_take + qs + E);
+            if (!(a_last > a_take + slack)) {
+                f.flags[j] = 1;
+                atomicAdd(f.flag_count, 1);
+            }
+        }
+    }
+    block_bitonic_sort(s2, P2);
+    if (threadIdx.x == 0) {
+        uint32_t *oi = f.out_ids + size_t(j) * f.k_out;
+        float *od = f.out_dists + size_t(j) * f.k_out;
+        int w = 0;
+        const uint32_t self0 = uint32_t(f.self_ids ? f.self_ids[j] : j + f.self_base);
+        bool dropped = !f.exclude_self;
+        const int limit = f.k_out + (f.exclude_self ? 1 : 0);
+        for (int i = 0; i < limit && i < P2 && w < f.k_out; ++i) {
+            const uint64_t key = s2[i];
+            if (!dropped && key != KEY_EMPTY && key_id0(key) == self0) { dropped = true; continue; }
+            if (key == KEY_EMPTY) { oi[w] = 0; od[w] = INFINITY; }
+            else { oi[w] = key_id0(key) + 1; od[w] = key_dist(key); }
+            ++w;
+        }
+        for (; w < f.k_out; ++w) { oi[w] = 0; od[w] = INFINITY; }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const float *db, const float *db_norm,
+                                   int64_t dim, const float *q, const float *q_norm, cudaStream_t st,
+                                   int *launches) {
+    const int P1 = next_pow2(int64_t(f.segs) * f.kk);
+    const int P2 = next_pow2(f.kk);
+    const size_t smem = size_t(P1 + P2) * 8;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (launches) *launches += 1;
+#define SSG_FR(MET)                                                                                      \
+    case MET: {                                                                                          \
+        cudaError_t e = cudaFuncSetAttribute(finalize_rerank_kernel<MET>,                                \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));   \
+        if (e != cudaSuccess) return e;                                                                  \
+        finalize_rerank_kernel<MET><<<unsigned(f.m), 128, smem, st>>>(f, db, db_norm, dim, q, q_norm, P1, P2); \
+        return cudaGetLastError();                                                                       \
+    }
+    switch (metric) {
+        SSG_FR(SQL2)
+        SSG_FR(L2)
+        SSG_FR(NORMCOSINE)
+        SSG_FR(COSINE)
+        SSG_FR(IP)
+        default: return cudaErrorInvalidValue;
+    }
+#undef SSG_FR
 }
 
 }  // namespace ssg

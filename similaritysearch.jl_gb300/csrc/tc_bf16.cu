@@ -1,0 +1,380 @@
+// tc_bf16.cu -- BF16 tensor-core distance tiles with a fused top-k (tcgen05).
+//
+// The reduced-precision method: distances between a tile of queries and a
+// tile of database rows are computed as one GEMM-shaped contraction on the
+// 5th-generation tensor cores (tcgen05.mma kind::f16, BF16 operands, FP32
+// accumulators in TMEM), turned into an approximate distance in the epilogue
+// and pushed into a per-query bounded top-k of kk = overfetch * k candidates.
+// The distance matrix never reaches HBM.  The candidates are then re-ranked
+// with the exact FP32 difference-form distance (finalize_rerank_kernel), so
+// the reported distances are the plain method's and the ids are exact
+// whenever the true neighbours survive the BF16 over-fetch.
+//
+// Data layout.  Queries and database rows are stored in HBM already in the
+// tensor core's operand layout: tiles of 128 rows, split along K into blocks
+// of 32 BF16 (64-byte rows) with the 64-byte swizzle applied, so one TMA bulk
+// copy (cp.async.bulk) of a tile lands in shared memory ready for the MMA --
+// no tensor map and no reformatting on chip.
+//
+// CTA roles (QT query tiles of 128 rows each, 64 + 128*QT threads):
+//   warp 0      TMA producer: the QT query tiles once, then database tiles
+//               through a STAGES-deep ring;
+//   warp 1      owns TMEM (2 x QT accumulators of 128 x 128 FP32) and issues
+//               the MMAs from one thread; accumulators are double-buffered so
+//               the epilogue of tile t overlaps the MMAs of tile t+1;
+//   warps 2..   epilogue: thread = one query row = one TMEM lane; reads its
+//               row 32 columns at a time (tcgen05.ld 32x32b.x32), filters
+//               against its heap frontier, and keeps its own top-kk heap in
+//               shared memory.
+// Every mbarrier wait is bounded (tc_ptx.cuh); a timeout sets *err and all
+// roles unwind, wait for their own in-flight copies/MMAs, free TMEM and exit.
+#include "common.cuh"
+#include "exact.cuh"
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+#include <cuda_bf16.h>
+
+namespace ssg {
+
+namespace {
+
+constexpr int TILE = 128;      // rows per query / database tile
+constexpr int SW = 64;         // bytes per swizzled K-block row (32 BF16)
+constexpr int KBE = SW / 2;    // BF16 elements per K-block
+
+enum { MC_DOT = 0, MC_SQ = 1, MC_COS = 2 };
+
+int metric_class(int metric) {
+    if (metric == SQL2 || metric == L2) return MC_SQ;
+    if (metric == COSINE) return MC_COS;
+    return MC_DOT;
+}
+
+// ---------------------------------------------------------------------------
+// Prep: FP32 rows -> BF16 tiles in the swizzled operand layout.
+// ---------------------------------------------------------------------------
+__global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kp, int64_t tiles,
+                                 uint8_t *__restrict__ out) {
+    const int chunks_per_row = kp / 8;
+    const int64_t total = tiles * TILE * chunks_per_row;
+    const size_t tile_bytes = size_t(TILE) * kp * 2;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        const int cidx = int(i % chunks_per_row);
+        const int64_t grow = i / chunks_per_row;
+        const int64_t tile = grow / TILE;
+        const int r = int(grow % TILE);
+        const int col0 = cidx * 8;
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            float f = 0.0f;
+            if (grow < rows && col0 + e < dim) f = x[grow * dim + col0 + e];
+            v[e] = __float2bfloat16_rn(f);
+        }
+        const int blk = col0 / KBE;
+        const uint32_t off = tc::swizzled_offset(uint32_t(r), uint32_t((col0 % KBE) * 2), SW);
+        uint8_t *dst = out + size_t(tile) * tile_bytes + size_t(blk) * TILE * SW + off;
+        *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(v);
+    }
+}
+
+// Per padded row: |x|^2 (MC_SQ) or 1/|x| (MC_COS), 0 for padding rows.
+__global__ void tc_norm_kernel(const float *__restrict__ x, int64_t rows, int dim, int64_t padded, int mc,
+                               float *__restrict__ out) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= padded) return;
+    float s = 0.0f;
+    if (i < rows) {
+        const float *r = x + i * dim;
+        for (int c = 0; c < dim; ++c) s = fmaf(r[c], r[c], s);
+    }
+    out[i] = (mc == MC_COS) ? (s > 0.0f ? 1.0f / sqrtf(s) : 0.0f) : s;
+}
+
+// ---------------------------------------------------------------------------
+// The scan.
+// ---------------------------------------------------------------------------
+struct TcArgs {
+    const uint8_t *qt;      // query tiles
+    const uint8_t *dt;      // database tiles
+    const float *dnorm;     // per padded database row (MC_SQ / MC_COS)
+    int64_t n;              // database rows
+    int64_t m;              // queries
+    int kp;                 // padded K (multiple of 32)
+    int kk;                 // candidates kept per query and split
+    int splits;
+    int64_t split_tiles;    // database tiles per split
+    int64_t n_tiles;
+    uint64_t *cand;
+    int *err;
+};
+
+template <int QT, int STAGES>
+struct TcSmem {
+    static size_t a_bytes(int kp) { return size_t(QT) * TILE * kp * 2; }
+    static size_t b_bytes(int kp) { return size_t(STAGES) * TILE * kp * 2; }
+    static size_t heap_bytes(int kk) { return size_t(QT) * TILE * kk * 8; }
+    static size_t bar_bytes() { return 256; }
+    static size_t total(int kp, int kk) { return 1024 + a_bytes(kp) + b_bytes(kp) + heap_bytes(kk) + bar_bytes(); }
+};
+
+template <int QT, int STAGES, int MC>
+__global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte alignment for the swizzle atoms
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const size_t tile_bytes = size_t(TILE) * a.kp * 2;
+    uint8_t *sA = smem;
+    uint8_t *sB = sA + QT * tile_bytes;
+    uint64_t *heap_base = reinterpret_cast<uint64_t *>(sB + STAGES * tile_bytes);
+    uint64_t *bars = heap_base + size_t(QT) * TILE * a.kk;
+    uint64_t *a_full = bars;
+    uint64_t *full = bars + 1;
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *mma_done = acc_empty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+
+    constexpr int NCOLS = QT * 2 * TILE;  // 256 or 512
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(a_full, 1);
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 4 * QT);
+        }
+        tc::mbar_init(mma_done, 1);
+        tc::fence_mbarrier_init();
+    }
+    if (warp == 1) tc::tmem_alloc<NCOLS>(tmem_slot);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    const int64_t t_lo = int64_t(blockIdx.y) * a.split_tiles;
+    int64_t t_hi = t_lo + a.split_tiles;
+    if (t_hi > a.n_tiles) t_hi = a.n_tiles;
+    const int T = t_hi > t_lo ? int(t_hi - t_lo) : 0;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tc::mbar_arrive_expect_tx(a_full, uint32_t(QT * tile_bytes));
+            for (int q = 0; q < QT; ++q)
+                tc::bulk_g2s(sA + q * tile_bytes, a.qt + (size_t(blockIdx.x) * QT + q) * tile_bytes,
+                             uint32_t(tile_bytes), a_full);
+            int issued = 0;
+            for (int t = 0; t < T; ++t) {
+                const int s = t % STAGES;
+                const uint32_t ph = (t / STAGES) & 1;
+                if (!tc::mbar_wait(&empty[s], ph ^ 1, a.err, 1)) break;
+                tc::mbar_arrive_expect_tx(&full[s], uint32_t(tile_bytes));
+                tc::bulk_g2s(sB + s * tile_bytes, a.dt + size_t(t_lo + t) * tile_bytes, uint32_t(tile_bytes),
+                             &full[s]);
+                issued = t + 1;
+            }
+            // wait (bounded) until every copy this thread issued has landed
+            tc::mbar_wait(a_full, 0, a.err, 2);
+            for (int t = issued - STAGES < 0 ? 0 : issued - STAGES; t < issued; ++t)
+                tc::mbar_wait(&full[t % STAGES], (t / STAGES) & 1, a.err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(TILE, TILE);
+            bool ok = tc::mbar_wait(a_full, 0, a.err, 3);
+            const uint32_t a_addr = tc::smem_u32(sA);
+            const uint32_t b_addr0 = tc::smem_u32(sB);
+            const int ksteps = a.kp / 16;
+            int issued = 0;
+            for (int t = 0; ok && t < T; ++t) {
+                const int s = t % STAGES;
+                const int b = t & 1;
+                if (!tc::mbar_wait(&full[s], (t / STAGES) & 1, a.err, 4)) break;
+                if (!tc::mbar_wait(&acc_empty[b], ((t >> 1) & 1) ^ 1, a.err, 5)) break;
+                tc::tc_fence_after();
+                const uint32_t b_addr = b_addr0 + uint32_t(s * tile_bytes);
+#pragma unroll
+                for (int q = 0; q < QT; ++q) {
+                    const uint32_t d_tmem = tmem_base + uint32_t((q * 2 + b) * TILE);
+                    for (int kk = 0; kk < ksteps; ++kk) {
+                        const uint32_t kbyte = uint32_t(kk) * 32u;
+                        const uint32_t blk_off = (kbyte / SW) * (TILE * SW) + (kbyte % SW);
+                        const uint64_t ad = tc::smem_desc(a_addr + uint32_t(q * tile_bytes) + blk_off, SW);
+                        const uint64_t bd = tc::smem_desc(b_addr + blk_off, SW);
+                        tc::mma_f16(d_tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+                    }
+                }
+                tc::mma_commit(&empty[s]);
+                tc::mma_commit(&acc_full[b]);
+                issued = t + 1;
+            }
+            (void)issued;
+            tc::mma_commit(mma_done);
+            tc::mbar_wait(mma_done, 0, a.err, 6);
+        }
+        __syncwarp();
+    } else {
+        const int e = warp - 2;
+        const int q = e / 4;
+        const int quarter = warp % 4;
+        const int row = quarter * 32 + lane;
+        const int64_t query = (int64_t(blockIdx.x) * QT + q) * TILE + row;
+        const int hs = QT * TILE;
+        Heap H{heap_base + (e * 32 + lane), a.kk, hs};
+        H.init();
+        uint64_t top = KEY_EMPTY;
+        float topd = INFINITY;
+        for (int t = 0; t < T; ++t) {
+            const int b = t & 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 7) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            tc::tc_fence_after();
+            const int64_t row0 = (t_lo + t) * TILE;
+#pragma unroll 1
+            for (int c = 0; c < TILE / 32; ++c) {
+                float v[32];
+                __syncwarp();
+                tc::tmem_ld_32x32b_x32(tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t((q * 2 + b) * TILE + c * 32),
+                                       v);
+                const int64_t id0 = row0 + c * 32;
+                const float *nrm = a.dnorm + id0;
+                float dmin = INFINITY;
+                float dv[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    float d;
+                    if (MC == MC_DOT) d = -v[j];
+                    else if (MC == MC_SQ) d = fmaf(-2.0f, v[j], __ldg(nrm + j));
+                    else d = -v[j] * __ldg(nrm + j);
+                    dv[j] = d;
+                    dmin = fminf(dmin, d);
+                }
+                if (dmin <= topd) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int64_t id = id0 + j;
+                        if (dv[j] <= topd && id < a.n) {
+                            const uint64_t key = make_key(dv[j], uint32_t(id));
+                            if (key < top) {
+                                top = H.replace_top(key);
+                                topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                            }
+                        }
+                    }
+                }
+            }
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        }
+        if (query < a.m) {
+            H.sort_ascending();
+            uint64_t *out = a.cand + (size_t(query) * a.splits + blockIdx.y) * a.kk;
+            for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc<NCOLS>(tmem_base);
+    }
+}
+
+template <int QT, int STAGES, int MC>
+cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
+    const size_t smem = TcSmem<QT, STAGES>::total(a.kp, a.kk);
+    auto kern = tc_scan_kernel<QT, STAGES, MC>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((a.m + QT * TILE - 1) / (QT * TILE)), unsigned(a.splits));
+    kern<<<grid, 64 + QT * TILE, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int QT, int STAGES>
+cudaError_t launch_tc_mc(const TcArgs &a, int mc, cudaStream_t st) {
+    if (mc == MC_SQ) return launch_tc_t<QT, STAGES, MC_SQ>(a, st);
+    if (mc == MC_COS) return launch_tc_t<QT, STAGES, MC_COS>(a, st);
+    return launch_tc_t<QT, STAGES, MC_DOT>(a, st);
+}
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host entry points.
+// ---------------------------------------------------------------------------
+int tc_padded_k(int64_t dim) { return int((dim + KBE - 1) / KBE * KBE); }
+int64_t tc_tiles(int64_t rows) { return (rows + TILE - 1) / TILE; }
+size_t tc_tile_bytes(int64_t dim) { return size_t(TILE) * tc_padded_k(dim) * 2; }
+
+// Picks (query tiles per CTA, stages) for this K and candidate count.
+bool tc_choose(int kp, int kk, int *qt, int *stages) {
+    if (TcSmem<2, 3>::total(kp, kk) <= kMaxSmem) { *qt = 2; *stages = 3; return true; }
+    if (TcSmem<1, 4>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 4; return true; }
+    if (TcSmem<1, 3>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 3; return true; }
+    if (TcSmem<1, 2>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 2; return true; }
+    return false;
+}
+
+cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
+                              cudaStream_t st, int *launches) {
+    const int kp = tc_padded_k(dim);
+    const int64_t total = tiles * TILE * (kp / 8);
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > 148 * 64) blocks = 148 * 64;
+    if (blocks < 1) blocks = 1;
+    if (launches) *launches += 1;
+    bf16_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kp, tiles, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,
+                            cudaStream_t st, int *launches) {
+    const int mc = metric_class(metric);
+    if (launches) *launches += 1;
+    tc_norm_kernel<<<unsigned((padded + 255) / 256), 256, 0, st>>>(x, rows, int(dim), padded, mc, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                           int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
+                           cudaStream_t st, int *launches, int *qt_out) {
+    TcArgs a{};
+    a.qt = q_tiles;
+    a.dt = d_tiles;
+    a.dnorm = d_norm;
+    a.n = n;
+    a.m = m;
+    a.kp = tc_padded_k(dim);
+    a.kk = kk;
+    a.splits = splits;
+    a.n_tiles = tc_tiles(n);
+    a.split_tiles = (a.n_tiles + splits - 1) / splits;
+    a.cand = cand;
+    a.err = err;
+    int qt = 0, stages = 0;
+    if (!tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
+    if (qt_out) *qt_out = qt;
+    if (launches) *launches += 1;
+    const int mc = metric_class(metric);
+    if (qt == 2) return launch_tc_mc<2, 3>(a, mc, st);
+    if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
+    if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
+    return launch_tc_mc<1, 2>(a, mc, st);
+}
+
+}  // namespace ssg

@@ -1,0 +1,127 @@
+"""GPU tests of the BF16 tensor-core method (tcgen05 scan + exact FP32 rerank).
+
+The method is approximate in which candidates survive the BF16 scan, exact in
+what it reports: every returned distance is the plain FP32 distance of the
+returned id (bit-identical to the oracle's sequential sum), rows are sorted
+by (distance, id), and recall@k against the FP64 oracle is stated per case.
+When the over-fetch keeps every database row, the result equals the plain
+method exactly.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_package
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NAMES = {"sql2": "SqL2", "l2": "L2", "normcosine": "NormCosine", "cosine": "Cosine", "ip": "InnerProduct"}
+
+
+@pytest.fixture(scope="module")
+def ss():
+    mod = load_package()
+    mod.build()
+    return mod
+
+
+def mixture(rng, n, d, centres=50, lo=0.1, hi=0.5, normalise=True):
+    C = rng.standard_normal((centres, d), dtype=np.float32)
+    sig = rng.uniform(lo, hi, size=centres).astype(np.float32)
+    lab = rng.integers(0, centres, size=n)
+    X = C[lab] + rng.standard_normal((n, d), dtype=np.float32) * sig[lab, None]
+    if normalise:
+        X /= np.linalg.norm(X, axis=1, keepdims=True)
+    return X.astype(np.float32)
+
+
+def run(ss, name, X, Q, k, **params):
+    idx = ss.GPUExhaustiveSearch(getattr(ss.Dist, NAMES[name])(), ss.MatrixDatabase.from_rows(X),
+                                 precision="bf16", **params)
+    ids, dists = ss.searchbatch(idx, ss.GenericContext(), ss.MatrixDatabase.from_rows(Q), k)
+    return np.ascontiguousarray(ids.T), np.ascontiguousarray(dists.T)
+
+
+def check_reported_distances_exact(name, X, Q, gi, gd):
+    for j in range(gi.shape[0]):
+        pairs = []
+        for t in range(gi.shape[1]):
+            i = int(gi[j, t])
+            assert i >= 1
+            d = np.float32(O.evaluate(name, X[i - 1], Q[j]))
+            assert gd[j, t] == d
+            pairs.append((float(d), i))
+        assert pairs == sorted(pairs)
+
+
+@pytest.mark.parametrize("name", ["sql2", "l2", "normcosine", "cosine", "ip"])
+@pytest.mark.parametrize("d", [32, 96, 100])
+def test_bf16_recall_and_exact_distances(ss, name, d):
+    rng = np.random.default_rng(d + len(name))
+    X = mixture(rng, 6000, d, normalise=(name != "ip" and name != "sql2" and name != "l2"))
+    Q = X[rng.integers(0, 6000, size=300)] + rng.standard_normal((300, d), dtype=np.float32) * 0.05
+    if name in ("normcosine",):
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    k = 10
+    gi, gd = run(ss, name, X, Q, k, overfetch=2.0)
+    check_reported_distances_exact(name, X, Q, gi[:40], gd[:40])
+    fi, _ = O.searchbatch_f64(name, X, Q, k)
+    assert O.macrorecall(fi, gi) >= 0.99
+
+
+def test_bf16_full_overfetch_equals_plain(ss):
+    # kk = n: every row is a candidate, the exact rerank decides everything
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((150, 96), dtype=np.float32)
+    Q = rng.standard_normal((200, 96), dtype=np.float32)
+    gi, gd = run(ss, "sql2", X, Q, 10, overfetch=64.0)
+    ri, rd = O.searchbatch("sql2", X, Q, 10)
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
+@pytest.mark.parametrize("splits", [1, 3, 8])
+def test_bf16_splits(ss, splits):
+    rng = np.random.default_rng(4)
+    X = mixture(rng, 9000, 64)
+    Q = X[:130] + rng.standard_normal((130, 64), dtype=np.float32) * 0.02
+    Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    gi, gd = run(ss, "normcosine", X, Q, 16, overfetch=2.0, splits=splits)
+    fi, _ = O.searchbatch_f64("normcosine", X, Q, 16)
+    assert O.macrorecall(fi, gi) >= 0.99
+    check_reported_distances_exact("normcosine", X, Q, gi[:20], gd[:20])
+
+
+@pytest.mark.parametrize("m", [1, 127, 128, 129, 257, 600])
+def test_bf16_query_counts(ss, m):
+    rng = np.random.default_rng(m)
+    X = mixture(rng, 3000, 96)
+    Q = X[rng.integers(0, 3000, size=m)]
+    gi, gd = run(ss, "normcosine", X, Q, 5, overfetch=2.0)
+    fi, _ = O.searchbatch_f64("normcosine", X, Q, 5)
+    assert O.macrorecall(fi, gi) >= 0.99
+
+
+def test_bf16_allknn_exclude_self(ss):
+    rng = np.random.default_rng(5)
+    X = mixture(rng, 5000, 96, centres=20)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.NormCosine(), ss.MatrixDatabase.from_rows(X), precision="bf16",
+                                 overfetch=1.5)
+    ids, dists = ss.allknn(idx, ss.GenericContext(), 32, exclude_self=True)
+    gi = np.ascontiguousarray(ids.T)
+    assert not np.any(gi == np.arange(1, 5001, dtype=np.uint32)[:, None])
+    rows = rng.choice(5000, size=300, replace=False)
+    fi, _ = O.searchbatch_f64("normcosine", X, X[rows], 33)
+    gold = np.zeros((300, 32), dtype=np.uint32)
+    for r, j in enumerate(rows):
+        keep = [t for t in range(33) if fi[r, t] != j + 1][:32]
+        gold[r] = fi[r, keep]
+    assert O.macrorecall(gold, gi[rows]) >= 0.99
+
+
+def test_bf16_rejects_hamming_and_large_dim(ss):
+    B = np.zeros((10, 2), dtype=np.uint64)
+    with pytest.raises(ss._native.UnsupportedError):
+        ss.GPUExhaustiveSearch(ss.Dist.Bits.Hamming(), ss.MatrixDatabase.from_rows(B), precision="bf16")
+    X = np.zeros((10, 300), dtype=np.float32)
+    with pytest.raises(ss._native.UnsupportedError):
+        ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X), precision="bf16")

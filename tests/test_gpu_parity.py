@@ -134,14 +134,45 @@ def test_large_k_uses_global_heaps(ss):
     assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
 
 
-def test_duplicates_break_ties_by_id(ss):
+@pytest.mark.parametrize("name", ["sql2", "l2", "normcosine"])
+def test_duplicates_break_ties_by_id(ss, name):
+    # 40 copies of every vector: ties at the k-th boundary everywhere.  For
+    # SqL2 / L2 the GEMM-form margin cannot be proven sufficient, so those
+    # queries must go through the exact fallback scan -- and still match.
     rng = np.random.default_rng(13)
     base = rng.standard_normal((50, 8), dtype=np.float32)
-    X = np.repeat(base, 40, axis=0)  # every vector 40 times
+    if name == "normcosine":
+        base /= np.linalg.norm(base, axis=1, keepdims=True)
+    X = np.repeat(base, 40, axis=0)
     rng.shuffle(X)
     Q = base[:10].copy()
-    gi, gd, _, _ = gpu_search(ss, ss.Dist.SqL2(), X, Q, 64)
-    ri, rd = O.searchbatch("sql2", X, Q, 64)
+    for k in (24, 64):  # 24: GEMM-form scan + fallback; 64: heaps exceed it -> exact scan
+        gi, gd, idx, _ = gpu_search(ss, dist_of(ss, name), X, Q, k)
+        ri, rd = O.searchbatch(name, X, Q, k)
+        assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+        if name != "normcosine" and k == 24:
+            assert idx.get_param("fallbacks") > 0
+
+
+@pytest.mark.parametrize("name", ["sql2", "l2", "normcosine", "cosine", "ip"])
+def test_exact_direct_scan_forced(ss, name):
+    # the exact direct scan (the fallback) on its own, every metric
+    rng = np.random.default_rng(21)
+    X = rng.standard_normal((2000, 45), dtype=np.float32)
+    Q = rng.standard_normal((70, 45), dtype=np.float32)
+    gi, gd, idx, _ = gpu_search(ss, dist_of(ss, name), X, Q, 12, exact_scan=1)
+    ri, rd = O.searchbatch(name, X, Q, 12)
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
+@pytest.mark.parametrize("margin", [1, 4, 64])
+def test_gemm_margin_is_self_checking(ss, margin):
+    # a tiny margin may fail the completeness check; results stay exact
+    rng = np.random.default_rng(22)
+    X = rng.standard_normal((3000, 33), dtype=np.float32)
+    Q = X[rng.integers(0, 3000, size=90)] + rng.standard_normal((90, 33), dtype=np.float32) * 1e-3
+    gi, gd, _, _ = gpu_search(ss, ss.Dist.SqL2(), X, Q, 10, margin=margin)
+    ri, rd = O.searchbatch("sql2", X, Q, 10)
     assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
 
 
