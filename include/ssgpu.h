@@ -143,6 +143,26 @@ void ssg_destroy(ssg_index *idx);
 /* ABI version (major * 10000 + minor * 100 + patch). */
 int ssg_version(void);
 
+/* Exact k-NN that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- programs
+ * whose own allocator already owns the GPU's memory, and request paths that
+ * must not allocate because cudaMalloc can synchronise the device.
+ * Database (n rows of dim Float32, or dim UInt64 words for HAMMING), queries
+ * (m rows) and results (m rows of k: 1-based ids, distances; 0 / +Inf when
+ * empty; (distance, id) order) are caller-owned device memory.  Metrics:
+ * SQL2, L2, NORMCOSINE, IP, HAMMING (COSINE returns SSG_EUNSUPPORTED).
+ * Results are those of ssg_search_device on the same data in the plain
+ * method.  The candidate scratch is a fixed 16 MiB array inside the library:
+ * m * min(k, n) must not exceed 2,097,152 (SSG_EINVAL otherwise).  The first
+ * call on a device looks up that array's address, so make it before any
+ * stream capture.  The work is enqueued on `stream` (a cudaStream_t, NULL =
+ * default stream) and the call returns without waiting for it.  All calls
+ * share the array: calls that overlap on the GPU race, calls ordered on one
+ * stream do not. */
+int ssg_knn_noalloc(int metric, const void *dev_db, int64_t dim, int64_t n,
+                    const void *dev_q, int64_t m, int32_t k,
+                    uint32_t *dev_ids, float *dev_dists, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,7 @@ SIGNATURES = {
     "ssg_set_stream": ([_p, _p], _int),
     "ssg_last_error": ([_p, C.c_char_p, _i64], _int),
     "ssg_destroy": ([_p], None),
+    "ssg_knn_noalloc": ([_int, _p, _i64, _i64, _p, _i64, _i32, _p, _p, _p], _int),
 }
 
 

@@ -724,6 +724,11 @@ int allknn_common(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *ids
 }  // namespace
 
 namespace ssg {
+int report_error(int code, const char *msg) {
+    snprintf(g_err, sizeof g_err, "%s", msg);
+    return code;
+}
+
 int device_sm_count() {
     static int cached[64] = {0};
     int dev = 0;

@@ -124,4 +124,8 @@ cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, 
 
 int device_sm_count();
 
+// Records `msg` as the calling thread's last error (what ssg_last_error(NULL,
+// ...) returns) and returns `code`.
+int report_error(int code, const char *msg);
+
 }  // namespace ssg

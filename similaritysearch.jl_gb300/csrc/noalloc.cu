@@ -1,0 +1,143 @@
+// noalloc.cu -- exact k-NN search that allocates no device memory.
+//
+// Who needs this.  Some callers cannot call cudaMalloc: an application whose
+// own allocator already owns the GPU's memory (a framework's caching pool that
+// reserves the device up front, so a second allocator would fail or fragment
+// it), and request paths that must not allocate because cudaMalloc can
+// synchronise the device and stall for milliseconds.  ssg_knn_noalloc serves
+// them: the caller passes the database, the queries and the result buffers
+// (all in device memory), and the only scratch the search needs -- the
+// candidate keys that the scan kernel hands to the merge kernel -- lives in a
+// fixed array compiled into this library.
+//
+// The array.  g_noalloc_keys is a file-scope __device__ array of
+// kNoAllocKeys 64-bit keys (16 MiB).  Every GPU that loads the library holds
+// it until the process exits.  Host code cannot use the array's name as a
+// device address (on the host it only names a stand-in), so the first call on
+// each device resolves the real address with cudaGetSymbolAddress while that
+// device is current and caches it; that first call should therefore come
+// before any stream capture.  Nothing in the array has to start at zero: the
+// scan writes every key slot the merge later reads.  All calls share the one
+// array and leave the last call's keys in it, so calls whose work overlaps on
+// the GPU (different streams, or several host threads without ordering) race;
+// calls issued in order on one stream do not.
+#include "../../include/ssgpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <mutex>
+
+namespace {
+
+constexpr int64_t kNoAllocKeys = int64_t(2) << 20;  // 2,097,152 keys = 16 MiB
+
+static __device__ __align__(256) uint64_t g_noalloc_keys[kNoAllocKeys];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+void *g_keys_addr[kMaxDevices] = {nullptr};
+
+int fail(int code, const char *fmt, long long a = 0, long long b = 0) {
+    char buf[512];
+    snprintf(buf, sizeof buf, fmt, a, b);
+    return ssg::report_error(code, buf);
+}
+
+// Device address of g_noalloc_keys on the current device (set up once).
+int keys_for_current_device(uint64_t **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(SSG_ECUDA, "no current CUDA device");
+    if (dev < 0 || dev >= kMaxDevices) return fail(SSG_EUNSUPPORTED, "device ordinal %lld out of range", dev);
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (!g_keys_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_keys);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return fail(SSG_ECUDA, "resolving the scratch array's device address failed");
+        }
+        g_keys_addr[dev] = p;
+    }
+    *out = static_cast<uint64_t *>(g_keys_addr[dev]);
+    return SSG_OK;
+}
+
+}  // namespace
+
+extern "C" int ssg_knn_noalloc(int metric, const void *dev_db, int64_t dim, int64_t n, const void *dev_q, int64_t m,
+                               int32_t k, uint32_t *dev_ids, float *dev_dists, void *stream) {
+    if (metric == SSG_METRIC_COSINE)
+        return fail(SSG_EUNSUPPORTED, "the no-allocation search supports SqL2, L2, NormCosine, InnerProduct and "
+                                      "Hamming (Cosine needs per-row norms, i.e. more scratch)");
+    if (metric < SSG_METRIC_SQL2 || metric > SSG_METRIC_HAMMING) return fail(SSG_EUNSUPPORTED, "unknown metric %lld", metric);
+    if (!dev_db || !dev_q || !dev_ids || !dev_dists) return fail(SSG_EINVAL, "NULL device pointer");
+    if (dim <= 0 || n <= 0 || m <= 0 || k <= 0)
+        return fail(SSG_EINVAL, "dim, n, m and k must be positive");
+    if (metric == SSG_METRIC_HAMMING && dim > 32)
+        return fail(SSG_EUNSUPPORTED, "Hamming sketches are limited to 32 words, got %lld", dim);
+    if (n >= (int64_t(1) << 32) - 1) return fail(SSG_EINVAL, "database length %lld out of range", n);
+    const int kk = int(std::min<int64_t>(k, n));
+    if (int64_t(m) * kk > kNoAllocKeys)
+        return fail(SSG_EINVAL,
+                    "m * min(k, n) = %lld candidate keys exceed the fixed scratch of %lld keys (16 MiB); "
+                    "split the query batch",
+                    (long long)(int64_t(m) * kk), (long long)kNoAllocKeys);
+
+    // splits: fill the GPU, keep splits long, stay inside the fixed scratch
+    const int64_t qtiles = (m + 127) / 128;
+    int64_t splits = (int64_t(4) * ssg::device_sm_count() + qtiles - 1) / qtiles;
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, n / std::max<int64_t>(1024, int64_t(8) * kk)));
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 8192 / kk));
+    splits = std::min<int64_t>(splits, kNoAllocKeys / (int64_t(m) * kk));
+    splits = std::max<int64_t>(1, splits);
+
+    ssg::ScanArgs a{};
+    a.metric = metric;
+    a.n = n;
+    a.dim = dim;
+    a.m = m;
+    a.kk = kk;
+    a.splits = int(splits);
+    a.split_len = (n + splits - 1) / splits;
+    a.id_base = 0;
+    const size_t gheap = metric == SSG_METRIC_HAMMING ? ssg::hamming_gheap_bytes(a) : ssg::direct_gheap_bytes(a);
+    if (gheap != 0)
+        return fail(SSG_EUNSUPPORTED, "k = %lld needs more top-k storage than shared memory holds "
+                                      "(the no-allocation search keeps its heaps on chip)", k);
+
+    uint64_t *keys = nullptr;
+    int rc = keys_for_current_device(&keys);
+    if (rc) return rc;
+    a.cand = keys;
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if (metric == SSG_METRIC_HAMMING)
+        e = ssg::launch_hamming(a, static_cast<const uint64_t *>(dev_db), static_cast<const uint64_t *>(dev_q), st,
+                                nullptr);
+    else
+        e = ssg::launch_direct_f32(a, static_cast<const float *>(dev_db), nullptr, static_cast<const float *>(dev_q),
+                                   nullptr, st, nullptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SSG_ECUDA, "launching the scan kernel failed");
+    }
+    ssg::FinalizeArgs f{};
+    f.cand = keys;
+    f.segs = int(splits);
+    f.kk = kk;
+    f.m = m;
+    f.k_out = k;
+    f.exclude_self = 0;
+    f.out_ids = dev_ids;
+    f.out_dists = dev_dists;
+    e = ssg::launch_finalize(f, st, nullptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SSG_ECUDA, "launching the merge kernel failed");
+    }
+    return SSG_OK;
+}
