@@ -224,6 +224,8 @@ def gpu_arm(args):
     N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, X.ctypes.data_as(C.c_void_p), d,
                          {"fp32": N.PREC_FP32, "bf16": N.PREC_BF16, "fp8": N.PREC_FP8}[mode], C.byref(h)))
     N.check(L.ssg_set_stream(h, C.c_void_p(stream.cuda_stream)), h)
+    if args.overfetch is not None:
+        N.check(L.ssg_set_param(h, b"overfetch", float(args.overfetch)), h)
     ids_d = torch.empty((n, K), dtype=torch.int32, device="cuda")
     dists_d = torch.empty((n, K), dtype=torch.float32, device="cuda")
 
@@ -282,6 +284,8 @@ def gpu_arm(args):
         N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, C.c_void_p(Xp.data_ptr()), d, prec,
                              C.byref(hh)))
         try:
+            if args.overfetch is not None:
+                N.check(L.ssg_set_param(hh, b"overfetch", float(args.overfetch)), hh)
             N.check(L.ssg_allknn(hh, K, 1, C.c_void_p(oi.data_ptr()), C.c_void_p(od.data_ptr())), hh)
         finally:
             L.ssg_destroy(hh)
@@ -374,6 +378,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DB,
                     help="database size (profiling captures use a smaller case of the same workload)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--overfetch", type=float, default=None,
+                    help="candidates per neighbour kept by the reduced-precision scan")
     args = ap.parse_args()
     N_DB = args.n
     if args.impl == "reference":

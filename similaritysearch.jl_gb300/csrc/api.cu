@@ -7,7 +7,7 @@
 // allknn! asserts 0 < k <= n, src/allknn.jl:73-75) and returns a status code
 // instead of throwing.  Nothing here falls back to a CPU path: every result is
 // produced by the kernels in this library.
-#include "../../include/ssgpu.h"
+#include "ssgpu.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -419,7 +419,7 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
     splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / kk));
     splits = std::max<int64_t>(1, splits);
     const int64_t split_len = (idx->n + splits - 1) / splits;
-    const int segs = int(splits) * 2;
+    const int segs = int(splits);
     const size_t per_query = size_t(segs) * kk * 8;
     int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
     chunk = std::min<int64_t>(chunk, m);
@@ -541,21 +541,24 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
     kk64 = std::max<int64_t>(kk64, take);
     kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
-    const int kk = int(kk64);
     const int kp = ssg::tc_padded_k(idx->dim);
+    // the over-fetch is capped by what the kernel's on-chip heaps hold
+    int kk = int(kk64);
     int qt = 0, stages = 0;
+    while (kk > take && !ssg::tc_choose(kp, kk, &qt, &stages)) --kk;
     if (!ssg::tc_choose(kp, kk, &qt, &stages))
-        return fail(idx, SSG_EUNSUPPORTED, "overfetch x k = %d candidates do not fit the BF16 kernel", kk);
+        return fail(idx, SSG_EUNSUPPORTED, "k = %d does not fit the BF16 kernel's on-chip top-k", take);
     const int64_t qrows = int64_t(qt) * 128;
     const int64_t qctas = (m + qrows - 1) / qrows;
     const int64_t n_tiles = ssg::tc_tiles(idx->n);
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
                                            : (ssg::device_sm_count() + qctas - 1) / qctas;
     splits = std::min<int64_t>(splits, n_tiles);
-    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 8192 / kk));
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / kk));
     splits = std::max<int64_t>(1, splits);
     // chunk the queries (a multiple of the CTA's query rows) to bound scratch
-    const size_t per_query = size_t(splits) * kk * 8;
+    const int segs = int(splits) * ssg::tc_segments_per_split(qt);
+    const size_t per_query = size_t(segs) * kk * 8;
     int64_t chunk = std::max<int64_t>(qrows, int64_t((size_t(1) << 30) / per_query) / qrows * qrows);
     chunk = std::min<int64_t>(chunk, (m + qrows - 1) / qrows * qrows);
     SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
@@ -583,7 +586,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
         f.cand = static_cast<const uint64_t *>(idx->cand.p);
-        f.segs = int(splits);
+        f.segs = segs;
         f.kk = kk;
         f.m = mc;
         f.k_out = k;

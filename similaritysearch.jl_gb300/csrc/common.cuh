@@ -115,6 +115,79 @@ struct Heap {
     }
 };
 
+// A thread-private top-kk heap fed through a small per-thread buffer.
+//
+// A candidate that beats the thread's (possibly stale) frontier is only
+// appended to the buffer; whenever any lane of the warp has `trigger` or more
+// buffered, the whole warp drains its buffers into its heaps together.  The
+// heap sift-downs of the 32 lanes then run side by side instead of one lane at
+// a time, which is what made per-candidate heap insertion slow: lanes of a
+// warp find candidates at different moments.  Every lane of the warp must
+// call maybe_drain() / drain() (lanes without a query simply offer nothing).
+struct BufferedTopK {
+    Heap H;
+    uint64_t *buf;  // per-thread buffer, `cap` entries with stride H.st
+    int c;
+    uint64_t top;
+    float topd;
+
+    __device__ __forceinline__ void init(uint64_t *heap, uint64_t *buffer, int kk, int st) {
+        H.h = heap;
+        H.kk = kk;
+        H.st = st;
+        H.init();
+        buf = buffer;
+        c = 0;
+        top = KEY_EMPTY;
+        topd = INFINITY;
+    }
+
+    // d passed the caller's prefilter (d <= topd) -- append it.
+    __device__ __forceinline__ void append(float d, uint32_t id) {
+        buf[c * H.st] = make_key(d, id);
+        ++c;
+    }
+
+    __device__ __forceinline__ void offer(float d, uint32_t id) {
+        if (d <= topd) append(d, id);
+    }
+
+    __device__ __forceinline__ void drain() {
+        int cmax = __reduce_max_sync(0xffffffffu, c);
+        for (int r = 0; r < cmax; ++r) {
+            if (r < c) {
+                const uint64_t key = buf[r * H.st];
+                if (key < top) top = H.replace_top(key);
+            }
+        }
+        c = 0;
+        topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+    }
+
+    __device__ __forceinline__ void maybe_drain(int trigger) {
+        if (__any_sync(0xffffffffu, c >= trigger)) drain();
+    }
+};
+
+// Drains the c keys buffered at buf (stride st) into the heap h and returns
+// the new top.  All 32 lanes of the warp call it together, so the lanes'
+// sift-downs run side by side.  Kept out of line so a kernel carries one copy
+// of the heap loop however many call sites it has (large unrolled epilogues
+// otherwise overflow the instruction cache); every argument is a scalar, so
+// the call needs no stack.
+static __device__ __noinline__ uint64_t heap_drain(uint64_t *h, const uint64_t *buf, int kk, int st, int c,
+                                            uint64_t top) {
+    const int cmax = __reduce_max_sync(0xffffffffu, c);
+    Heap H{h, kk, st};
+    for (int r = 0; r < cmax; ++r) {
+        if (r < c) {
+            const uint64_t key = buf[r * st];
+            if (key < top) top = H.replace_top(key);
+        }
+    }
+    return top;
+}
+
 // Bitonic sort of P (a power of two) keys in shared memory by the whole block.
 __device__ __forceinline__ void block_bitonic_sort(uint64_t *s, int P) {
     for (int size = 2; size <= P; size <<= 1) {

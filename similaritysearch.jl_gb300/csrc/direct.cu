@@ -26,6 +26,8 @@ namespace {
 
 constexpr int TN = 32;  // database rows per tile (accumulators per thread)
 constexpr int KC = 32;  // dims per shared-memory chunk
+constexpr int kBufCap = 12;      // buffered top-k: drain checked every 8 values, trigger 4
+constexpr int kDrainTrigger = 4;
 
 template <int METRIC>
 __device__ __forceinline__ float finish(float acc, float xnorm, float qnorm) {
@@ -51,7 +53,7 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
     float(*xs)[KC] = reinterpret_cast<float(*)[KC]>(smem + size_t(KC) * (QPB + 1) * 4);
     uint64_t *hbase = heap_in_smem
         ? reinterpret_cast<uint64_t *>(smem + direct_static_smem<QPB>())
-        : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk) * QPB;
+        : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk + kBufCap) * QPB;
 
     const int t = threadIdx.x;
     const int64_t q0 = int64_t(blockIdx.x) * QPB;
@@ -61,10 +63,8 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
     const int64_t hi = lo + a.split_len < a.n ? lo + a.split_len : a.n;
     const int dim = int(a.dim);
 
-    Heap H{hbase + t, a.kk, QPB};
-    H.init();
-    uint64_t top = KEY_EMPTY;
-    float topd = INFINITY;
+    BufferedTopK T;
+    T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
     const float qnorm = (METRIC == COSINE && qvalid) ? qn[qi] : 1.0f;
 
     for (int64_t j0 = lo; j0 < hi; j0 += TN) {
@@ -109,23 +109,21 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
                 }
             }
         }
-        if (qvalid) {
 #pragma unroll
-            for (int j = 0; j < TN; ++j) {
+        for (int g = 0; g < TN; g += 8) {
+#pragma unroll
+            for (int j = g; j < g + 8; ++j) {
                 const int64_t id = j0 + j;
-                if (id < hi) {
+                if (qvalid && id < hi) {
                     const float d = finish<METRIC>(acc[j], METRIC == COSINE ? xn[id] : 1.0f, qnorm);
-                    if (d <= topd) {
-                        const uint64_t key = make_key(d, uint32_t(id + a.id_base));
-                        if (key < top) {
-                            top = H.replace_top(key);
-                            topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                        }
-                    }
+                    if (d <= T.topd) T.append(d, uint32_t(id + a.id_base));
                 }
             }
+            T.maybe_drain(kDrainTrigger);
         }
     }
+    T.drain();
+    Heap &H = T.H;
     if (qvalid) {
         H.sort_ascending();
         uint64_t *out = a.cand + (size_t(qi) * a.splits + blockIdx.y) * a.kk;
@@ -137,14 +135,14 @@ constexpr size_t kSmemBudget = 200 * 1024;
 
 template <int QPB>
 bool heap_fits(int kk) {
-    return direct_static_smem<QPB>() + size_t(kk) * QPB * 8 <= kSmemBudget;
+    return direct_static_smem<QPB>() + size_t(kk + kBufCap) * QPB * 8 <= kSmemBudget;
 }
 
 template <int METRIC, int QPB>
 cudaError_t launch_direct_t(const ScanArgs &a, const float *db, const float *xn, const float *q,
                             const float *qn, cudaStream_t st) {
     const bool in_smem = heap_fits<QPB>(a.kk);
-    size_t smem = direct_static_smem<QPB>() + (in_smem ? size_t(a.kk) * QPB * 8 : 0);
+    size_t smem = direct_static_smem<QPB>() + (in_smem ? size_t(a.kk + kBufCap) * QPB * 8 : 0);
     auto kern = direct_f32_kernel<METRIC, QPB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -162,7 +160,7 @@ size_t direct_gheap_bytes(const ScanArgs &a) {
     bool fits = qpb == 128 ? heap_fits<128>(a.kk) : heap_fits<32>(a.kk);
     if (fits) return 0;
     size_t blocks = size_t((a.m + qpb - 1) / qpb) * a.splits;
-    return blocks * size_t(a.kk) * qpb * 8;
+    return blocks * size_t(a.kk + kBufCap) * qpb * 8;
 }
 
 cudaError_t launch_direct_f32(const ScanArgs &a, const float *db, const float *db_norm,

@@ -3,18 +3,20 @@
 // The plain method's fast path.  A CTA computes a 128-query x 128-row tile
 // of dot products with 8x8 accumulators per thread (FFMA, k in index order,
 // so every dot product is the same fma chain as search(::ExhaustiveSearch)'s
-// `d = muladd(a_i, b_i, d)`, src/dist/cos.jl:78-84), stages the tile in
-// shared memory and lets each thread push half a row into its private top-k
-// heap.
+// `d = muladd(a_i, b_i, d)`, src/dist/cos.jl:78-84).  Operand slices of 16
+// dims are copied global -> shared with 4-byte cp.async straight into the
+// k-major layout the inner loop reads (double-buffered), so no registers are
+// spent on staging and two CTAs fit on an SM.  After the last slice the tile
+// is staged in two 64-row halves through the operand buffers; thread r
+// (r < 128) owns query row r and pushes its 128 values into its top-k.
 //   * NormCosine / InnerProduct / Cosine: the tile values ARE the exact FP32
 //     distances (1 - dot, -dot, 1 - dot / (|x| |q|)), so the keys are final.
 //   * SqL2 / L2: the tile holds |x|^2 - 2 x.q (the query's |q|^2 is common to
 //     the row and dropped).  That GEMM form differs from the reference's
 //     difference form sum (x_i - q_i)^2 (src/dist/vecs.jl:93-102) by
 //     rounding, so kk = k + margin candidates are kept and re-scored exactly
-//     in finalize_rerank_kernel, which also checks that the margin provably
-//     covers the exact top k (see rerank_check below) and flags the query
-//     for the exact direct scan otherwise.
+//     in finalize_rerank_kernel, which checks that the margin provably covers
+//     the exact top k and flags the query for the exact direct scan otherwise.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -25,16 +27,19 @@ namespace {
 constexpr int BM = 128;       // queries per CTA
 constexpr int BN = 128;       // database rows per tile
 constexpr int BK = 16;        // dims per pipeline stage
-constexpr int PAD = 4;        // smem row padding (floats)
-constexpr int LDA = BM + PAD;
-constexpr int SROW = BN + PAD;  // staged tile row stride
+constexpr int LDA = BM + 4;   // padded k-major row (floats)
+constexpr int SROW = BN + 4;  // staged tile row stride (floats)
 constexpr int THREADS = 256;
+constexpr int STAGES = 3;         // cp.async pipeline depth (slices in flight)
+constexpr int kBufCap = 12;       // buffered top-k: drain checked every 8 values, trigger 4
+constexpr int kDrainTrigger = 4;
+
+static_assert(STAGES * 2 * BK * LDA >= (BM / 2) * SROW, "a staged half tile must fit the operand buffers");
 
 struct GemmSmem {
-    static size_t operands() { return size_t(2) * BK * (LDA + LDA) * 4; }
-    static size_t stage() { return size_t(BM) * SROW * 4; }
-    static size_t heaps(int kk) { return size_t(THREADS) * kk * 8; }
-    static size_t total(int kk) { return operands() + stage() + heaps(kk); }
+    __host__ __device__ static constexpr size_t operands() { return size_t(STAGES) * 2 * BK * LDA * 4; }
+    static size_t heaps(int kk) { return size_t(BM) * (kk + kBufCap) * 8; }
+    static size_t total(int kk) { return operands() + heaps(kk); }
 };
 
 template <int METRIC>
@@ -45,38 +50,45 @@ __device__ __forceinline__ float gemm_value(float acc, float xaux, float qn) {
     return fmaf(-2.0f, acc, xaux);  // SQL2 / L2: |x|^2 - 2 x.q
 }
 
-// Loads the BK-wide k-slice [k0, k0+BK) of 128 rows (rows >= rows_valid or
-// columns >= dim read as 0) into registers: thread -> (row = tid/2, 8 dims).
-__device__ __forceinline__ void load_slice(const float *__restrict__ base, int64_t row0, int64_t rows_valid,
-                                           int dim, int k0, float (&r)[8]) {
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+    const int sz = valid ? 4 : 0;  // src-size 0: the 4 bytes are zero-filled
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// all but the most recently committed group are complete
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Issues the copies of the k-slice [k0, k0+BK) of 128 rows of `base` into the
+// k-major buffer s (s[k][row]); rows >= rows_valid or dims >= dim are zeros.
+// Thread -> (row = tid / 2, 8 consecutive dims).
+__device__ __forceinline__ void load_slice_async(float *s, const float *__restrict__ base, int64_t row0,
+                                                 int64_t rows_valid, int dim, int k0) {
     const int tid = threadIdx.x;
     const int row = tid >> 1;
     const int c0 = (tid & 1) * 8;
     const int64_t gr = row0 + row;
+    const bool rv = gr < rows_valid;
+    const float *src = base + (rv ? gr : 0) * dim;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int c = k0 + c0 + i;
-        r[i] = (gr < rows_valid && c < dim) ? base[gr * dim + c] : 0.0f;
+        const bool v = rv && c < dim;
+        cp_async4(s + (c0 + i) * LDA + row, v ? src + c : base, v);
     }
 }
 
-__device__ __forceinline__ void store_slice(float *__restrict__ s, const float (&r)[8]) {
-    const int tid = threadIdx.x;
-    const int row = tid >> 1;
-    const int c0 = (tid & 1) * 8;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) s[(c0 + i) * LDA + row] = r[i];
-}
-
 template <int METRIC>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, 2)
 gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restrict__ xaux,
                 const float *__restrict__ Q, const float *__restrict__ qn) {
     extern __shared__ __align__(16) unsigned char smem[];
-    float *sA = reinterpret_cast<float *>(smem);            // [2][BK][LDA]
-    float *sB = sA + 2 * BK * LDA;                           // [2][BK][LDA]
-    float *sT = sB + 2 * BK * LDA;                           // [BM][SROW]
-    uint64_t *heaps = reinterpret_cast<uint64_t *>(sT + BM * SROW);
+    float *sA = reinterpret_cast<float *>(smem);  // [STAGES][BK][LDA]
+    float *sB = sA + STAGES * BK * LDA;            // [STAGES][BK][LDA]
+    float *sT = sA;                                // staged half tile [64][SROW], aliases the operands
+    uint64_t *heaps = reinterpret_cast<uint64_t *>(smem + GemmSmem::operands());
+    uint64_t *bufs = heaps + size_t(BM) * a.kk;
 
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
@@ -85,14 +97,11 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
     const int64_t hi = lo + a.split_len < a.n ? lo + a.split_len : a.n;
     const int dim = int(a.dim);
 
-    // heap owner: query row hq, columns [hh*64, hh*64+64)
-    const int hq = tid >> 1, hh = tid & 1;
-    Heap H{heaps + tid, a.kk, THREADS};
-    H.init();
-    uint64_t top = KEY_EMPTY;
-    float topd = INFINITY;
-    const bool hq_valid = q0 + hq < a.m;
-    const float hqn = (METRIC == COSINE && hq_valid) ? qn[q0 + hq] : 1.0f;
+    // thread r < 128 owns query row r (warps 0-3)
+    const bool owner = tid < BM;
+    const bool row_valid = owner && q0 + tid < a.m;
+    BufferedTopK T;
+    if (owner) T.init(heaps + tid, bufs + tid, a.kk, BM);
 
     for (int64_t j0 = lo; j0 < hi; j0 += BN) {
         float acc[8][8];
@@ -101,20 +110,27 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
 #pragma unroll
             for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 
-        float ra[8], rb[8];
-        load_slice(Q, q0, a.m, dim, 0, ra);
-        load_slice(db, j0, hi, dim, 0, rb);
         __syncthreads();  // the previous tile's epilogue is done with shared memory
-        store_slice(sA, ra);
-        store_slice(sB, rb);
-        __syncthreads();
-        int buf = 0;
-        for (int k0 = 0; k0 < dim; k0 += BK) {
-            const bool more = k0 + BK < dim;
-            if (more) {
-                load_slice(Q, q0, a.m, dim, k0 + BK, ra);
-                load_slice(db, j0, hi, dim, k0 + BK, rb);
+        const int nslices = (dim + BK - 1) / BK;
+        // prologue: slices 0 and 1 in flight (one commit group each, maybe empty)
+        load_slice_async(sA, Q, q0, a.m, dim, 0);
+        load_slice_async(sB, db, j0, hi, dim, 0);
+        cp_async_commit();
+        if (nslices > 1) {
+            load_slice_async(sA + BK * LDA, Q, q0, a.m, dim, BK);
+            load_slice_async(sB + BK * LDA, db, j0, hi, dim, BK);
+        }
+        cp_async_commit();
+        for (int sl = 0; sl < nslices; ++sl) {
+            cp_async_wait_one();
+            __syncthreads();  // slice sl visible; the buffer of slice sl-1 is free
+            if (sl + 2 < nslices) {
+                const int nb = (sl + 2) % STAGES;
+                load_slice_async(sA + nb * BK * LDA, Q, q0, a.m, dim, (sl + 2) * BK);
+                load_slice_async(sB + nb * BK * LDA, db, j0, hi, dim, (sl + 2) * BK);
             }
+            cp_async_commit();
+            const int buf = sl % STAGES;
             const float *cA = sA + buf * BK * LDA;
             const float *cB = sB + buf * BK * LDA;
 #pragma unroll
@@ -130,61 +146,58 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
 #pragma unroll
                     for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(bv[j], av[i], acc[i][j]);
             }
-            if (more) {
-                store_slice(sA + (buf ^ 1) * BK * LDA, ra);
-                store_slice(sB + (buf ^ 1) * BK * LDA, rb);
+        }
+        cp_async_wait_all();
+        // epilogue, in two halves of 64 query rows staged through the operands
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            __syncthreads();  // operands (or the previous half) no longer read
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int lr = ty * 4 + i;        // row within the half
+                const int qr = h * 64 + lr;       // query row within the tile
+                const float qq = (METRIC == COSINE && q0 + qr < a.m) ? qn[q0 + qr] : 1.0f;
+#pragma unroll
+                for (int hc = 0; hc < 2; ++hc) {
+                    const int cb = hc * 64 + tx * 4;
+                    float4 v;
+                    float *pv = reinterpret_cast<float *>(&v);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int64_t id = j0 + cb + j;
+                        const float aux = (METRIC == NORMCOSINE || METRIC == IP) ? 0.0f
+                                          : (id < hi ? xaux[id] : 0.0f);
+                        pv[j] = gemm_value<METRIC>(acc[h * 4 + i][hc * 4 + j], aux, qq);
+                    }
+                    *reinterpret_cast<float4 *>(sT + lr * SROW + cb) = v;
+                }
             }
             __syncthreads();
-            buf ^= 1;
-        }
-        // stage the tile: row = query, column = database row
+            // warps 2h and 2h+1 own rows [64h, 64h + 64)
+            if ((tid >> 6) == h) {
+                const float *row = sT + (tid - h * 64) * SROW;
+#pragma unroll 2
+                for (int c = 0; c < BN; c += 8) {
+                    const float4 v0 = *reinterpret_cast<const float4 *>(row + c);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(row + c + 4);
+                    const float vv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int qr = (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int cb = h * 64 + tx * 4;
-                float4 v;
-                float *pv = reinterpret_cast<float *>(&v);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int64_t id = j0 + cb + j;
-                    const float aux = (METRIC == NORMCOSINE || METRIC == IP) ? 0.0f
-                                      : (id < hi ? xaux[id] : 0.0f);
-                    const float qq = (METRIC == COSINE && q0 + qr < a.m) ? qn[q0 + qr] : 1.0f;
-                    pv[j] = gemm_value<METRIC>(acc[i][h * 4 + j], aux, qq);
-                }
-                *reinterpret_cast<float4 *>(sT + qr * SROW + cb) = v;
-            }
-        }
-        __syncthreads();
-        if (hq_valid) {
-            const float *row = sT + hq * SROW + hh * 64;
-            const int64_t idb = j0 + hh * 64;
-#pragma unroll 4
-            for (int c = 0; c < 64; c += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(row + c);
-                const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int64_t id = idb + c + j;
-                    if (vv[j] <= topd && id < hi) {
-                        const uint64_t key = make_key(vv[j], uint32_t(id + a.id_base));
-                        if (key < top) {
-                            top = H.replace_top(key);
-                            topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                        }
+                    for (int j = 0; j < 8; ++j) {
+                        const int64_t id = j0 + c + j;
+                        if (row_valid && vv[j] <= T.topd && id < hi) T.append(vv[j], uint32_t(id + a.id_base));
                     }
+                    T.maybe_drain(kDrainTrigger);
                 }
             }
         }
-        (void)hqn;
     }
-    if (hq_valid) {
-        H.sort_ascending();
-        // segments per query: splits x 2 halves
-        uint64_t *out = a.cand + ((size_t(q0 + hq) * a.splits + blockIdx.y) * 2 + hh) * a.kk;
-        for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * THREADS];
+    if (owner) {
+        T.drain();
+        if (row_valid) {
+            T.H.sort_ascending();
+            uint64_t *out = a.cand + (size_t(q0 + tid) * a.splits + blockIdx.y) * a.kk;
+            for (int i = 0; i < a.kk; ++i) out[i] = T.H.h[i * BM];
+        }
     }
 }
 

@@ -20,6 +20,8 @@ namespace ssg {
 namespace {
 
 constexpr int TN = 64;
+constexpr int kBufCap = 12;      // buffered top-k: drain checked every 8 values, trigger 4
+constexpr int kDrainTrigger = 4;
 
 template <int WMAX, int QPB>
 __host__ __device__ constexpr size_t ham_static_smem() {
@@ -34,7 +36,7 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
     uint64_t(*xs)[WMAX] = reinterpret_cast<uint64_t(*)[WMAX]>(smem);
     uint64_t *hbase = heap_in_smem
         ? reinterpret_cast<uint64_t *>(smem + ham_static_smem<WMAX, QPB>())
-        : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk) * QPB;
+        : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk + kBufCap) * QPB;
 
     const int t = threadIdx.x;
     const int W = int(a.dim);
@@ -47,10 +49,8 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
 #pragma unroll
     for (int w = 0; w < WMAX; ++w) q[w] = (qvalid && w < W) ? Q[qi * W + w] : 0ull;
 
-    Heap H{hbase + t, a.kk, QPB};
-    H.init();
-    uint64_t top = KEY_EMPTY;
-    int topd = 0x7fffffff;
+    BufferedTopK T;
+    T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
 
     for (int64_t j0 = lo; j0 < hi; j0 += TN) {
         __syncthreads();
@@ -60,24 +60,24 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
             xs[r][c] = (xr < hi && c < W) ? db[xr * W + c] : 0ull;
         }
         __syncthreads();
-        if (!qvalid) continue;
         const int jn = hi - j0 < TN ? int(hi - j0) : TN;
-        for (int j = 0; j < jn; ++j) {
-            int d = 0;
+        for (int g = 0; g < jn; g += 8) {
+            const int ge = g + 8 < jn ? g + 8 : jn;
+            for (int j = g; j < ge; ++j) {
+                int d = 0;
 #pragma unroll
-            for (int w = 0; w < WMAX; w += 2) {
-                const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(&xs[j][w]);
-                d += __popcll(q[w] ^ x.x) + __popcll(q[w + 1] ^ x.y);
-            }
-            if (d <= topd) {
-                const uint64_t key = make_key(float(d), uint32_t(j0 + j + a.id_base));
-                if (key < top) {
-                    top = H.replace_top(key);
-                    topd = (top == KEY_EMPTY) ? 0x7fffffff : int(key_dist(top));
+                for (int w = 0; w < WMAX; w += 2) {
+                    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(&xs[j][w]);
+                    d += __popcll(q[w] ^ x.x) + __popcll(q[w + 1] ^ x.y);
                 }
+                const float fd = float(d);
+                if (qvalid && fd <= T.topd) T.append(fd, uint32_t(j0 + j + a.id_base));
             }
+            T.maybe_drain(kDrainTrigger);
         }
     }
+    T.drain();
+    Heap &H = T.H;
     if (qvalid) {
         H.sort_ascending();
         uint64_t *out = a.cand + (size_t(qi) * a.splits + blockIdx.y) * a.kk;
@@ -89,7 +89,7 @@ constexpr size_t kSmemBudget = 200 * 1024;
 
 template <int WMAX, int QPB>
 bool ham_heap_fits(int kk) {
-    return ham_static_smem<WMAX, QPB>() + size_t(kk) * QPB * 8 <= kSmemBudget;
+    return ham_static_smem<WMAX, QPB>() + size_t(kk + kBufCap) * QPB * 8 <= kSmemBudget;
 }
 
 template <int WMAX>
@@ -98,7 +98,7 @@ int ham_qpb(int kk) { return ham_heap_fits<WMAX, 128>(kk) ? 128 : 32; }
 template <int WMAX, int QPB>
 cudaError_t launch_ham_t(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
     const bool in_smem = ham_heap_fits<WMAX, QPB>(a.kk);
-    size_t smem = ham_static_smem<WMAX, QPB>() + (in_smem ? size_t(a.kk) * QPB * 8 : 0);
+    size_t smem = ham_static_smem<WMAX, QPB>() + (in_smem ? size_t(a.kk + kBufCap) * QPB * 8 : 0);
     auto kern = hamming_kernel<WMAX, QPB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -118,7 +118,7 @@ size_t ham_gheap(const ScanArgs &a) {
     int qpb = ham_qpb<WMAX>(a.kk);
     bool fits = qpb == 128 ? ham_heap_fits<WMAX, 128>(a.kk) : ham_heap_fits<WMAX, 32>(a.kk);
     if (fits) return 0;
-    return size_t((a.m + qpb - 1) / qpb) * a.splits * size_t(a.kk) * qpb * 8;
+    return size_t((a.m + qpb - 1) / qpb) * a.splits * size_t(a.kk + kBufCap) * qpb * 8;
 }
 
 }  // namespace

@@ -89,6 +89,9 @@ int64_t tc_tiles(int64_t rows);
 size_t tc_tile_bytes(int64_t dim);
 // Chooses query tiles per CTA and pipeline depth; false if kk cannot fit.
 bool tc_choose(int kp, int kk, int *qt, int *stages);
+// Sorted candidate segments the scan writes per (query, split) for a CTA with
+// `qt` query tiles (the epilogue splits a tile's columns between warps).
+int tc_segments_per_split(int qt);
 cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
                               cudaStream_t st, int *launches);
 // |x|^2 (SqL2/L2) or 1/|x| (Cosine) per padded row.
@@ -105,7 +108,7 @@ cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const floa
                                    int *launches);
 
 // ---- plain FP32 GEMM-form scan (gemm_f32.cu) ----
-// Writes splits x 2 sorted segments of kk keys per query.
+// Writes `splits` sorted segments of kk keys per query.
 bool gemm_fits(int kk);
 cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
                             const float *q_norm, cudaStream_t st, int *launches);

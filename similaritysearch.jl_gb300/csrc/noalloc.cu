@@ -21,7 +21,7 @@
 // array and leave the last call's keys in it, so calls whose work overlaps on
 // the GPU (different streams, or several host threads without ordering) race;
 // calls issued in order on one stream do not.
-#include "../../include/ssgpu.h"
+#include "ssgpu.h"
 #include "common.cuh"
 #include "kernels.h"
 

@@ -45,6 +45,21 @@ constexpr int KBE = SW / 2;    // BF16 elements per K-block
 
 enum { MC_DOT = 0, MC_SQ = 1, MC_COS = 2 };
 
+// Per-thread candidate buffer in front of the heap: drains are checked after
+// every 8 columns with a trigger of 4, so at most 3 + 8 entries are pending.
+constexpr int kBufCap = 12;
+constexpr int kDrainTrigger = 4;
+constexpr int kDrainEvery = 8;
+
+// Column splits of the epilogue: with one query tile per CTA, two warps share
+// each TMEM lane quarter and filter half of the tile's columns each (two heaps
+// per query, merged later), so every scheduler has two epilogue warps to
+// overlap latencies.
+template <int QT>
+__host__ __device__ constexpr int col_splits() { return QT == 1 ? 2 : 1; }
+template <int QT>
+__host__ __device__ constexpr int tc_threads() { return 64 + TILE * QT * col_splits<QT>(); }
+
 int metric_class(int metric) {
     if (metric == SQL2 || metric == L2) return MC_SQ;
     if (metric == COSINE) return MC_COS;
@@ -115,13 +130,14 @@ template <int QT, int STAGES>
 struct TcSmem {
     static size_t a_bytes(int kp) { return size_t(QT) * TILE * kp * 2; }
     static size_t b_bytes(int kp) { return size_t(STAGES) * TILE * kp * 2; }
-    static size_t heap_bytes(int kk) { return size_t(QT) * TILE * kk * 8; }
+    static size_t heap_bytes(int kk) { return size_t(QT) * TILE * col_splits<QT>() * (kk + kBufCap) * 8; }
     static size_t bar_bytes() { return 256; }
     static size_t total(int kp, int kk) { return 1024 + a_bytes(kp) + b_bytes(kp) + heap_bytes(kk) + bar_bytes(); }
 };
 
 template <int QT, int STAGES, int MC>
-__global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
+__global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) {
+    constexpr int CS = col_splits<QT>();
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -129,7 +145,8 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
     uint8_t *sA = smem;
     uint8_t *sB = sA + QT * tile_bytes;
     uint64_t *heap_base = reinterpret_cast<uint64_t *>(sB + STAGES * tile_bytes);
-    uint64_t *bars = heap_base + size_t(QT) * TILE * a.kk;
+    uint64_t *buf_base = heap_base + size_t(QT) * TILE * CS * a.kk;
+    uint64_t *bars = buf_base + size_t(QT) * TILE * CS * kBufCap;
     uint64_t *a_full = bars;
     uint64_t *full = bars + 1;
     uint64_t *empty = full + STAGES;
@@ -150,7 +167,7 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 4 * QT);
+            tc::mbar_init(&acc_empty[b], 4 * QT * CS);
         }
         tc::mbar_init(mma_done, 1);
         tc::fence_mbarrier_init();
@@ -164,7 +181,7 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
     const int64_t t_lo = int64_t(blockIdx.y) * a.split_tiles;
     int64_t t_hi = t_lo + a.split_tiles;
     if (t_hi > a.n_tiles) t_hi = a.n_tiles;
-    const int T = t_hi > t_lo ? int(t_hi - t_lo) : 0;
+    const int T_tiles = t_hi > t_lo ? int(t_hi - t_lo) : 0;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -173,7 +190,7 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
                 tc::bulk_g2s(sA + q * tile_bytes, a.qt + (size_t(blockIdx.x) * QT + q) * tile_bytes,
                              uint32_t(tile_bytes), a_full);
             int issued = 0;
-            for (int t = 0; t < T; ++t) {
+            for (int t = 0; t < T_tiles; ++t) {
                 const int s = t % STAGES;
                 const uint32_t ph = (t / STAGES) & 1;
                 if (!tc::mbar_wait(&empty[s], ph ^ 1, a.err, 1)) break;
@@ -195,7 +212,7 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
             const uint32_t b_addr0 = tc::smem_u32(sB);
             const int ksteps = a.kp / 16;
             int issued = 0;
-            for (int t = 0; ok && t < T; ++t) {
+            for (int t = 0; ok && t < T_tiles; ++t) {
                 const int s = t % STAGES;
                 const int b = t & 1;
                 if (!tc::mbar_wait(&full[s], (t / STAGES) & 1, a.err, 4)) break;
@@ -224,63 +241,86 @@ __global__ void __launch_bounds__(64 + QT * 128, 1) tc_scan_kernel(TcArgs a) {
         __syncwarp();
     } else {
         const int e = warp - 2;
-        const int q = e / 4;
+        const int q = e / (4 * CS);
+        const int cs = (e / 4) % CS;
         const int quarter = warp % 4;
         const int row = quarter * 32 + lane;
         const int64_t query = (int64_t(blockIdx.x) * QT + q) * TILE + row;
-        const int hs = QT * TILE;
-        Heap H{heap_base + (e * 32 + lane), a.kk, hs};
-        H.init();
+        constexpr int hs = QT * TILE * CS;
+        constexpr int CHUNKS = TILE / 32 / CS;  // 32-column chunks per warp and tile
+        uint64_t *heap = heap_base + (e * 32 + lane);
+        uint64_t *cbuf = buf_base + (e * 32 + lane);
+        Heap{heap, a.kk, hs}.init();
         uint64_t top = KEY_EMPTY;
         float topd = INFINITY;
-        for (int t = 0; t < T; ++t) {
+        int nbuf = 0;
+        for (int t = 0; t < T_tiles; ++t) {
             const int b = t & 1;
             int ok = 1;
             if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 7) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
-            const int64_t row0 = (t_lo + t) * TILE;
-#pragma unroll 1
-            for (int c = 0; c < TILE / 32; ++c) {
-                float v[32];
-                __syncwarp();
-                tc::tmem_ld_32x32b_x32(tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t((q * 2 + b) * TILE + c * 32),
-                                       v);
+            const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
+            // this warp's columns in flight together, one wait, then the
+            // accumulator goes back to the MMA warp before any filtering
+            uint32_t r[CHUNKS][32];
+            __syncwarp();
+            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) +
+                                   uint32_t((q * 2 + b) * TILE + cs * (TILE / CS));
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) tc::tmem_ld_32x32b_x32_async(tbase + uint32_t(c * 32), r[c]);
+            tc::tmem_wait_ld();
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) {
                 const int64_t id0 = row0 + c * 32;
                 const float *nrm = a.dnorm + id0;
-                float dmin = INFINITY;
+                // approximate distance of each column and its minimum per
+                // group of 8 columns (DOT ranks by -v: take the maximum of v)
                 float dv[32];
+                float gmin[4];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    float d;
-                    if (MC == MC_DOT) d = -v[j];
-                    else if (MC == MC_SQ) d = fmaf(-2.0f, v[j], __ldg(nrm + j));
-                    else d = -v[j] * __ldg(nrm + j);
-                    dv[j] = d;
-                    dmin = fminf(dmin, d);
+                for (int g = 0; g < 4; ++g) {
+                    float m = MC == MC_DOT ? -INFINITY : INFINITY;
+#pragma unroll
+                    for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                        const float v = __uint_as_float(r[c][j]);
+                        if (MC == MC_DOT) { dv[j] = v; m = fmaxf(m, v); }
+                        else if (MC == MC_SQ) { dv[j] = fmaf(-2.0f, v, __ldg(nrm + j)); m = fminf(m, dv[j]); }
+                        else { dv[j] = -v * __ldg(nrm + j); m = fminf(m, dv[j]); }
+                    }
+                    gmin[g] = MC == MC_DOT ? -m : m;
                 }
-                if (dmin <= topd) {
+                const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+                if (__any_sync(0xffffffffu, dmin <= topd)) {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int64_t id = id0 + j;
-                        if (dv[j] <= topd && id < a.n) {
-                            const uint64_t key = make_key(dv[j], uint32_t(id));
-                            if (key < top) {
-                                top = H.replace_top(key);
-                                topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                            }
+                    for (int g = 0; g < 4; ++g) {
+                        if (!__any_sync(0xffffffffu, gmin[g] <= topd)) continue;
+#pragma unroll
+                        for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                            // branch-free append: the slot is always written,
+                            // the count only advances for a candidate
+                            const float d = MC == MC_DOT ? -dv[j] : dv[j];
+                            cbuf[nbuf * hs] = make_key(d, uint32_t(id0 + j));
+                            nbuf += (d <= topd && id0 + j < a.n) ? 1 : 0;
+                        }
+                        if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
+                            top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+                            nbuf = 0;
+                            topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
                         }
                     }
                 }
             }
-            tc::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
         }
+        top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        Heap H{heap, a.kk, hs};
         if (query < a.m) {
             H.sort_ascending();
-            uint64_t *out = a.cand + (size_t(query) * a.splits + blockIdx.y) * a.kk;
+            uint64_t *out = a.cand + ((size_t(query) * a.splits + blockIdx.y) * CS + cs) * a.kk;
             for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
         }
     }
@@ -299,7 +339,7 @@ cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + QT * TILE - 1) / (QT * TILE)), unsigned(a.splits));
-    kern<<<grid, 64 + QT * TILE, smem, st>>>(a);
+    kern<<<grid, tc_threads<QT>(), smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -318,12 +358,15 @@ constexpr size_t kMaxSmem = 227 * 1024;
 // Host entry points.
 // ---------------------------------------------------------------------------
 int tc_padded_k(int64_t dim) { return int((dim + KBE - 1) / KBE * KBE); }
+int tc_segments_per_split(int qt) { return qt == 1 ? col_splits<1>() : col_splits<2>(); }
 int64_t tc_tiles(int64_t rows) { return (rows + TILE - 1) / TILE; }
 size_t tc_tile_bytes(int64_t dim) { return size_t(TILE) * tc_padded_k(dim) * 2; }
 
 // Picks (query tiles per CTA, stages) for this K and candidate count.
 bool tc_choose(int kp, int kk, int *qt, int *stages) {
-    if (TcSmem<2, 3>::total(kp, kk) <= kMaxSmem) { *qt = 2; *stages = 3; return true; }
+    // One query tile per CTA with eight epilogue warps measured faster than two
+    // query tiles with four warps each (the epilogue, not the database
+    // traffic, limits the scan), so only QT = 1 is used.
     if (TcSmem<1, 4>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 4; return true; }
     if (TcSmem<1, 3>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 3; return true; }
     if (TcSmem<1, 2>::total(kp, kk) <= kMaxSmem) { *qt = 1; *stages = 2; return true; }
@@ -353,6 +396,7 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out) {
+    // (qt_out receives the query tiles per CTA; segments per split follow from it)
     TcArgs a{};
     a.qt = q_tiles;
     a.dt = d_tiles;
@@ -371,7 +415,6 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     if (qt_out) *qt_out = qt;
     if (launches) *launches += 1;
     const int mc = metric_class(metric);
-    if (qt == 2) return launch_tc_mc<2, 3>(a, mc, st);
     if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
     if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
     return launch_tc_mc<1, 2>(a, mc, st);

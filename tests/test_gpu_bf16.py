@@ -72,7 +72,7 @@ def test_bf16_recall_and_exact_distances(ss, name, d):
 def test_bf16_full_overfetch_equals_plain(ss):
     # kk = n: every row is a candidate, the exact rerank decides everything
     rng = np.random.default_rng(3)
-    X = rng.standard_normal((150, 96), dtype=np.float32)
+    X = rng.standard_normal((100, 96), dtype=np.float32)
     Q = rng.standard_normal((200, 96), dtype=np.float32)
     gi, gd = run(ss, "sql2", X, Q, 10, overfetch=64.0)
     ri, rd = O.searchbatch("sql2", X, Q, 10)
