@@ -1,9 +1,16 @@
 """Benchmark of the exhaustive k-NN path on GB300.
 
-Workload (one step): allknn self-join with NormCosine over n = 1,000,000
-Float32 vectors of d = 96 drawn from a 1,000-cluster Gaussian mixture
-(centres N(0,1), per-cluster sigma U[0.1, 0.5]) and L2-normalised; k = 32
-neighbours excluding the object itself.  Inputs are seeded synthetic data.
+Headline workload (one step): allknn self-join with NormCosine over
+n = 1,000,000 Float32 vectors of d = 96 drawn from a 1,000-cluster Gaussian
+mixture (centres N(0,1), per-cluster sigma U[0.1, 0.5]) and L2-normalised;
+k = 32 neighbours excluding the object itself.  Inputs are seeded synthetic
+data of the shapes the benchmark names (no dataset is involved).
+
+The metric is queries/s at recall@10 >= 0.99: the headline `value` is the
+reduced-precision method (BF16 tensor-core distances over-fetching
+1.25 x (k+1) candidates, re-ranked in exact FP32), whose recall against the
+oracle is measured on a sample of rows in the same run; `modes.fp32` is the
+plain FP32 method on the same data (same results as ExhaustiveSearch).
 
 Arms:
   default            the GPU engine (libssgpu.so) -- prints one JSON line
@@ -12,10 +19,15 @@ Arms:
                      reference cannot run on this machine), timed on a bounded
                      sample of the same workload
 
-The timed device region has the database resident in HBM (384 MB, larger than
-the 129 MB L2, so no flush is needed between steps).  ``e2e`` repeats the step
-through the public C ABI from pinned host memory: upload the database, run
-allknn, read the (k, n) ids and distances back.
+Other workloads of the benchmark suite (`--workload c1|c3`) print a line of
+the same shape: C1 searchbatch SqL2 (d=128, n=100,000, m=1,000, k=10) and C3
+Hamming (2,000,000 sketches of 1,024 bits, 10,000 queries at 10 % bit flips,
+k=100).
+
+The timed device region has the database resident in HBM (the C2 database is
+384 MB FP32, larger than the 129 MB L2, so no flush is needed between steps).
+``e2e`` repeats the step through the public C ABI from pinned host memory:
+upload the database, run the search, read the (k, n) ids and distances back.
 """
 from __future__ import annotations
 
@@ -39,6 +51,12 @@ N_DB = 1_000_000
 DIM = 96
 K = 32
 N_CENTRES = 1000
+HEADLINE_MODE = "bf16"
+HEADLINE_OVERFETCH = 1.25
+
+METRIC = "queries/s @ recall@10>=0.99 (allknn NormCosine n=1e6 d=96 k=32 excl. self)"
+DATA = ("synthetic: seeded 1000-cluster Gaussian mixture (centres N(0,1), sigma U[0.1,0.5]), "
+        "L2-normalised, n=1,000,000, d=96")
 
 
 def load_package():
@@ -123,6 +141,45 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def roofline_flops(mode, flops_per_launch, avg_launch_ms):
+    """Roofline of a contraction kernel from its algorithmic flops per launch."""
+    pk = peaks()
+    achieved = flops_per_launch / (avg_launch_ms / 1e3) / 1e12
+    if mode == "fp32":
+        sm_max = pk.get("sm_max_mhz", 2070.0)
+        # FP32 SIMT peak: 152 SMs x 128 lanes x 2 flop x the measured max SM clock
+        peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        note = "FP32 SIMT nominal at the measured max SM clock (152x128x2xclk): no measured FP32 peak exists"
+        bound = "fp32"
+    else:
+        peak = pk.get("bf16_tflops", 1900.0)
+        note = "bf16_tflops of measured" if "bf16_tflops" in pk else "bf16 fallback 1.9 PF"
+        bound = "tensor"
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "scan", "per_launch_ms": avg_launch_ms,
+            "flops_per_launch": flops_per_launch, "peak_note": note}
+
+
+def roofline_bytes(bytes_per_launch, avg_launch_ms):
+    pk = peaks()
+    achieved = bytes_per_launch / (avg_launch_ms / 1e3) / 1e9
+    peak = pk.get("hbm_gbs", 6800.0)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "scan", "per_launch_ms": avg_launch_ms, "bytes_per_launch": bytes_per_launch,
+            "peak_note": "hbm_gbs of measured" if "hbm_gbs" in pk else "hbm fallback 6.8 TB/s"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle restatement (baseline and reference arm)
+# ---------------------------------------------------------------------------
+
 def cpu_baseline(X: np.ndarray, budget_s: float = 12.0, rows=None):
     """Times the oracle's allknn restatement (ExhaustiveSearch semantics,
     @simd-style 16-lane sums, all host threads) on a sample of query rows."""
@@ -179,191 +236,310 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmean * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
-        "config": config_dict("fp32"),
+        "config": config_dict(HEADLINE_MODE, HEADLINE_OVERFETCH),
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-METRIC = "queries/s @ recall@10>=0.99 (allknn NormCosine n=1e6 d=96 k=32 excl. self)"
-DATA = ("synthetic: seeded 1000-cluster Gaussian mixture (centres N(0,1), sigma U[0.1,0.5]), "
-        "L2-normalised, n=1,000,000, d=96")
-
-
-def config_dict(mode):
+def config_dict(mode, overfetch):
     return {"workload": "allknn self-join NormCosine, n=1,000,000, d=96, k=32 excluding self",
             "n": N_DB, "d": DIM, "k": K, "exclude_self": True, "mode": mode,
+            "overfetch": overfetch if mode != "fp32" else None,
             "l2_policy": "inputs larger than L2 (384 MB database > 129 MB L2); no flush",
             "parallelism": "replicas only (one independent index per GPU)"}
 
 
-def gpu_arm(args):
-    import torch
-    import torch.distributed as dist
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+class Ctx:
+    def __init__(self):
+        import torch
+        import torch.distributed as dist
+        self.torch, self.dist = torch, dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        if self.world > 1:
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+        ss = load_package()
+        ss.build()
+        self.N = ss._native
+        self.L = self.N.lib()
 
-    ss = load_package()
-    ss.build()
-    N = ss._native
-    L = N.lib()
+    def max_over_ranks(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([v], device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
 
-    X = make_mixture(N_DB)
-    n, d = X.shape
-    mode = args.mode
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
 
-    # --- device-resident timing -------------------------------------------------
+
+PREC = {"fp32": 0, "bf16": 1, "fp8": 2}
+
+
+def timed_device_steps(cx, h, step, steps, warmup):
+    """W untimed + K timed steps on the library's stream (torch's current
+    stream); returns (ms per step max over ranks, launches, scan ms, scan launches, clocks)."""
+    torch, N, L = cx.torch, cx.N, cx.L
     stream = torch.cuda.current_stream()
-    h = C.c_void_p()
-    N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, X.ctypes.data_as(C.c_void_p), d,
-                         {"fp32": N.PREC_FP32, "bf16": N.PREC_BF16, "fp8": N.PREC_FP8}[mode], C.byref(h)))
-    N.check(L.ssg_set_stream(h, C.c_void_p(stream.cuda_stream)), h)
-    if args.overfetch is not None:
-        N.check(L.ssg_set_param(h, b"overfetch", float(args.overfetch)), h)
-    ids_d = torch.empty((n, K), dtype=torch.int32, device="cuda")
-    dists_d = torch.empty((n, K), dtype=torch.float32, device="cuda")
-
-    def step():
-        N.check(L.ssg_allknn_device(h, K, 1, C.c_void_p(ids_d.data_ptr()), C.c_void_p(dists_d.data_ptr())), h)
-
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     N.check(L.ssg_set_param(h, b"profile", 1.0), h)
-    if world > 1:
-        dist.barrier()
+    cx.barrier()
     torch.cuda.synchronize()
     launches = 0
-    with ClockSampler(local) as clk:
+    with ClockSampler(cx.local) as clk:
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
             v = C.c_double()
             L.ssg_get_param(h, b"kernel_launches", C.byref(v))
             launches += int(v.value)
         e1.record(stream)
         torch.cuda.synchronize()
-    t_ms = e0.elapsed_time(e1)
-    if world > 1:
-        dist.barrier()
+    t_ms = cx.max_over_ranks(e0.elapsed_time(e1))
+    cx.barrier()
     v = C.c_double()
     L.ssg_get_param(h, b"main_kernel_ms", C.byref(v))
     main_ms = v.value
     L.ssg_get_param(h, b"main_kernel_launches", C.byref(v))
     main_launches = int(v.value)
     N.check(L.ssg_set_param(h, b"profile", 0.0), h)
+    return t_ms / steps, launches, main_ms, main_launches, clk.summary()
 
-    t_max = t_ms
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    ms_per_step = t_max / args.steps
-    qps = world * n * args.steps / (t_max / 1e3)
 
+def allknn_mode(cx, X, mode, overfetch, steps, warmup):
+    torch, N, L = cx.torch, cx.N, cx.L
+    n, d = X.shape
+    h = C.c_void_p()
+    N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, X.ctypes.data_as(C.c_void_p), d, PREC[mode],
+                         C.byref(h)))
+    N.check(L.ssg_set_stream(h, C.c_void_p(torch.cuda.current_stream().cuda_stream)), h)
+    if mode != "fp32" and overfetch is not None:
+        N.check(L.ssg_set_param(h, b"overfetch", float(overfetch)), h)
+    ids_d = torch.empty((n, K), dtype=torch.int32, device="cuda")
+    dists_d = torch.empty((n, K), dtype=torch.float32, device="cuda")
+
+    def step():
+        N.check(L.ssg_allknn_device(h, K, 1, C.c_void_p(ids_d.data_ptr()), C.c_void_p(dists_d.data_ptr())), h)
+
+    ms, launches, main_ms, main_launches, clocks = timed_device_steps(cx, h, step, steps, warmup)
     ids_host = ids_d.cpu().numpy().view(np.uint32)
-    dists_host = dists_d.cpu().numpy()
     L.ssg_destroy(h)
+    avg = main_ms / max(1, main_launches)
+    q_per_launch = n * steps / max(1, main_launches)
+    roof = roofline_flops(mode, 2.0 * q_per_launch * n * d, avg)
+    return {"ms_per_step": ms, "qps": cx.world * n / (ms / 1e3), "launches": launches, "roofline": roof,
+            "clocks": clocks, "ids": ids_host}
 
-    # --- end to end through the C ABI from pinned host memory -------------------
+
+def allknn_e2e(cx, X, mode, overfetch, steps):
+    torch, N, L = cx.torch, cx.N, cx.L
+    n, d = X.shape
     Xp = torch.from_numpy(X).pin_memory()
     oi = torch.empty((n, K), dtype=torch.int32).pin_memory()
     od = torch.empty((n, K), dtype=torch.float32).pin_memory()
-    prec = {"fp32": N.PREC_FP32, "bf16": N.PREC_BF16, "fp8": N.PREC_FP8}[mode]
 
     def e2e_step():
         hh = C.c_void_p()
-        N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, C.c_void_p(Xp.data_ptr()), d, prec,
+        N.check(L.ssg_create(N.METRIC_NORMCOSINE, N.ELEM_F32, d, n, C.c_void_p(Xp.data_ptr()), d, PREC[mode],
                              C.byref(hh)))
         try:
-            if args.overfetch is not None:
-                N.check(L.ssg_set_param(hh, b"overfetch", float(args.overfetch)), hh)
+            if mode != "fp32" and overfetch is not None:
+                N.check(L.ssg_set_param(hh, b"overfetch", float(overfetch)), hh)
             N.check(L.ssg_allknn(hh, K, 1, C.c_void_p(oi.data_ptr()), C.c_void_p(od.data_ptr())), hh)
         finally:
             L.ssg_destroy(hh)
 
-    e2e_steps = max(1, min(args.steps, 3))
     e2e_step()
-    if world > 1:
-        dist.barrier()
+    cx.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_qps = world * n * e2e_steps / e2e_s
+    s = cx.max_over_ranks(time.perf_counter() - t0)
+    return {"value": cx.world * n * steps / s, "unit": "queries/s", "h2d_bytes_per_step": int(X.nbytes),
+            "d2h_bytes_per_step": int(n * K * 8), "steps": steps}
 
-    if rank != 0:
-        if world > 1:
-            dist.destroy_process_group()
-        return
 
-    # --- roofline of the dominant (scan) kernel ---------------------------------
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    sm_max = peaks.get("sm_max_mhz", 2070.0)
-    avg_launch_ms = main_ms / max(1, main_launches)
-    queries_per_launch = n * args.steps / max(1, main_launches)
-    flops_per_launch = 2.0 * queries_per_launch * n * d
-    achieved = flops_per_launch / (avg_launch_ms / 1e3) / 1e12
-    if mode == "fp32":
-        # FP32 SIMT peak: 152 SMs x 128 lanes x 2 flop x max SM clock (no measured FP32 peak exists)
-        peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-        peak_note = "FP32 SIMT nominal at measured max SM clock (152x128x2xclk); not a measured copy/GEMM peak"
-    else:
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_note = "bf16_tflops of measured" if "bf16_tflops" in peaks else "bf16 fallback 1.9 PF"
-    roof = {"bound": "tensor" if mode != "fp32" else "fp32", "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None, "kernel": "scan",
-            "per_launch_ms": avg_launch_ms, "flops_per_launch": flops_per_launch, "peak_note": peak_note}
-
-    # --- CPU baseline + recall on the sampled rows --------------------------------
-    if args.skip_cpu:
-        print(json.dumps({"metric": METRIC, "value": qps, "unit": "queries/s", "n": n,
-                          "ms_per_step": ms_per_step, "roofline": roof, "gpu_launches": launches}), flush=True)
-        return
-    cpu, rows, cids, cdists = cpu_baseline(X, budget_s=args.cpu_budget)
-    # exclude self from the oracle rows like the GPU did
-    gold = np.zeros((rows.size, K), dtype=np.uint32)
-    for r, j in enumerate(rows):
+def recall_vs(gold_rows, cids, got):
+    """recall@10 / recall@32 of GPU rows against oracle rows (self removed)."""
+    gold = np.zeros((gold_rows.size, K), dtype=np.uint32)
+    for r, j in enumerate(gold_rows):
         keep = [t for t in range(K + 1) if cids[r, t] != j + 1][:K]
         gold[r] = cids[r, keep]
-    got = ids_host[rows]
-    rec10 = float(np.mean([len(set(gold[r, :10]) & set(got[r, :10])) / 10 for r in range(rows.size)]))
-    rec32 = float(np.mean([len(set(gold[r]) & set(got[r])) / K for r in range(rows.size)]))
+    g = got[gold_rows]
+    r10 = float(np.mean([len(set(gold[r, :10]) & set(g[r, :10])) / 10 for r in range(gold_rows.size)]))
+    r32 = float(np.mean([len(set(gold[r]) & set(g[r])) / K for r in range(gold_rows.size)]))
+    return r10, r32
+
+
+def gpu_arm(args):
+    cx = Ctx()
+    X = make_mixture(N_DB)
+    n = X.shape[0]
+    mode = args.mode
+    of = args.overfetch if args.overfetch is not None else HEADLINE_OVERFETCH
+    head = allknn_mode(cx, X, mode, of, args.steps, args.warmup)
+    if args.skip_cpu:
+        if cx.rank == 0:
+            print(json.dumps({"metric": METRIC, "value": head["qps"], "unit": "queries/s", "n": n, "mode": mode,
+                              "ms_per_step": head["ms_per_step"], "roofline": head["roofline"],
+                              "gpu_launches": head["launches"]}), flush=True)
+        return
+    e2e = allknn_e2e(cx, X, mode, of, max(1, min(args.steps, 3)))
+    modes = {mode: {"value": head["qps"], "ms_per_step": head["ms_per_step"], "roofline_frac":
+                    head["roofline"]["frac"]}}
+    plain = None
+    if mode != "fp32" and not args.no_plain:
+        plain = allknn_mode(cx, X, "fp32", None, 1, 1)
+        modes["fp32"] = {"value": plain["qps"], "ms_per_step": plain["ms_per_step"],
+                         "roofline": plain["roofline"], "note": "plain FP32 method, 1 warm-up + 1 timed step"}
+    if cx.rank != 0:
+        return
+    cpu, rows, cids, _ = cpu_baseline(X, budget_s=args.cpu_budget)
+    r10, r32 = recall_vs(rows, cids, head["ids"])
+    modes[mode]["recall@10"], modes[mode]["recall@32"] = r10, r32
+    if plain is not None:
+        p10, p32 = recall_vs(rows, cids, plain["ids"])
+        modes["fp32"]["recall@10"], modes["fp32"]["recall@32"] = p10, p32
+        modes["speedup_vs_fp32"] = head["qps"] / plain["qps"]
     line = {
-        "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": head["qps"], "unit": "queries/s", "n_gpus": cx.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if mode == "fp32" else mode, "data": DATA,
-        "config": config_dict(mode),
-        "recall": {"recall@10": rec10, "recall@32": rec32, "sample_rows": int(rows.size),
+        "config": config_dict(mode, of),
+        "recall": {"recall@10": r10, "recall@32": r32, "sample_rows": int(rows.size),
                    "gold": "oracle ExhaustiveSearch restatement (FP32, 16-lane sums)"},
-        "roofline": roof,
+        "roofline": head["roofline"],
         "cpu_baseline": {k: v for k, v in cpu.items() if k != "seconds"},
-        "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(X.nbytes),
-                "d2h_bytes_per_step": int(n * K * 8), "steps": e2e_steps},
-        "clocks": clk.summary(),
-        "gpu_launches": launches,
+        "e2e": e2e,
+        "clocks": head["clocks"],
+        "gpu_launches": head["launches"],
+        "modes": modes,
     }
     print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    if cx.world > 1:
+        cx.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# Other workloads of the suite: C1 (SqL2 searchbatch) and C3 (Hamming)
+# ---------------------------------------------------------------------------
+
+def make_c1():
+    X = np.random.default_rng(1).standard_normal((100_000, 128), dtype=np.float32)
+    Q = np.random.default_rng(2).standard_normal((1_000, 128), dtype=np.float32)
+    return X, Q, 10
+
+
+def make_c3(n=2_000_000, m=10_000):
+    W = 16
+    X = np.random.default_rng(6).integers(0, 2**64 - 1, size=(n, W), dtype=np.uint64, endpoint=True)
+    src = np.random.default_rng(7).integers(0, n, size=m)
+    flips = np.random.default_rng(8).random((m, W * 64)) < 0.1
+    mask = np.ascontiguousarray(np.packbits(flips, axis=1)).view(np.uint64)
+    return X, X[src] ^ mask, 100
+
+
+def workload_arm(args):
+    cx = Ctx()
+    torch, N, L = cx.torch, cx.N, cx.L
+    from oracle import oracle as O
+    if args.workload == "c1":
+        X, Q, k = make_c1()
+        metric, elem, mname = N.METRIC_SQL2, N.ELEM_F32, "sql2"
+        desc = "searchbatch SqL2, n=100,000, d=128, m=1,000, k=10 (N(0,1) data)"
+    else:
+        X, Q, k = make_c3(args.n if args.n is not None else 2_000_000)
+        metric, elem, mname = N.METRIC_HAMMING, N.ELEM_U64, "hamming"
+        desc = f"searchbatch Bits.Hamming, n={X.shape[0]:,} sketches x 1024 bits, m=10,000 (10% flips), k=100"
+    mode = args.mode if args.workload == "c1" else "fp32"
+    n, d = X.shape
+    m = Q.shape[0]
+    h = C.c_void_p()
+    N.check(L.ssg_create(metric, elem, d, n, X.ctypes.data_as(C.c_void_p), d, PREC[mode], C.byref(h)))
+    N.check(L.ssg_set_stream(h, C.c_void_p(torch.cuda.current_stream().cuda_stream)), h)
+    if mode != "fp32" and args.overfetch is not None:
+        N.check(L.ssg_set_param(h, b"overfetch", float(args.overfetch)), h)
+    Qd = torch.from_numpy(Q.view(np.int64) if Q.dtype == np.uint64 else Q).cuda()
+    ids_d = torch.empty((m, k), dtype=torch.int32, device="cuda")
+    dists_d = torch.empty((m, k), dtype=torch.float32, device="cuda")
+
+    def step():
+        N.check(L.ssg_search_device(h, C.c_void_p(Qd.data_ptr()), m, k, C.c_void_p(ids_d.data_ptr()),
+                                    C.c_void_p(dists_d.data_ptr()), 0), h)
+
+    ms, launches, main_ms, main_launches, clocks = timed_device_steps(cx, h, step, args.steps, args.warmup)
+    gi = ids_d.cpu().numpy().view(np.uint32)
+    gd = dists_d.cpu().numpy()
+    L.ssg_destroy(h)
+    avg = main_ms / max(1, main_launches)
+    if args.workload == "c1":
+        roof = roofline_flops(mode, 2.0 * m * n * d, avg)
+    else:
+        # one pass over the sketches + the queries + the results (bytes per call)
+        roof = roofline_bytes(8.0 * d * n + 8.0 * d * m + 8.0 * k * m, avg)
+        roof["popcount_words_per_s"] = n * m * d / (avg / 1e3)
+    # e2e: create from host + search from host + results to host
+    Xp = torch.from_numpy(X.view(np.int64) if X.dtype == np.uint64 else X).pin_memory()
+    Qp = torch.from_numpy(Q.view(np.int64) if Q.dtype == np.uint64 else Q).pin_memory()
+    oi = torch.empty((m, k), dtype=torch.int32).pin_memory()
+    od = torch.empty((m, k), dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        hh = C.c_void_p()
+        N.check(L.ssg_create(metric, elem, d, n, C.c_void_p(Xp.data_ptr()), d, PREC[mode], C.byref(hh)))
+        try:
+            if mode != "fp32" and args.overfetch is not None:
+                N.check(L.ssg_set_param(hh, b"overfetch", float(args.overfetch)), hh)
+            N.check(L.ssg_search(hh, C.c_void_p(Qp.data_ptr()), d, m, k, C.c_void_p(oi.data_ptr()),
+                                 C.c_void_p(od.data_ptr()), 0), hh)
+        finally:
+            L.ssg_destroy(hh)
+
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / 2
+    # CPU baseline + parity on a sample of queries (oracle restatement)
+    threads = os.cpu_count() or 1
+    sample = np.random.default_rng(23).choice(m, size=min(m, args.cpu_queries), replace=False)
+    t0 = time.perf_counter()
+    ri, rd = O.searchbatch(mname, X, Q[sample], k, lanes=16 if mname != "hamming" else 1, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    parity = {"sample_queries": int(sample.size),
+              "ids_equal": bool(np.array_equal(gi[sample], ri)) if mname == "hamming" else None,
+              "dists_equal": bool(np.array_equal(gd[sample], rd)) if mname == "hamming" else None,
+              "recall@k": O.macrorecall(ri, gi[sample])}
+    if mname != "hamming":
+        parity["max_rel_ddist"] = float(np.max(np.abs(gd[sample] - rd) / np.maximum(np.abs(rd), 1.0)))
+    line = {"metric": f"queries/s ({args.workload})", "value": m / (ms / 1e3), "unit": "queries/s",
+            "n_gpus": cx.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64" if mname == "hamming" else ("f32" if mode == "fp32" else mode),
+            "data": "synthetic, seeded", "config": {"workload": desc, "mode": mode},
+            "roofline": roof, "parity": parity,
+            "cpu_baseline": {"value": sample.size / cpu_s, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample.size} queries against all {n:,} objects, oracle C restatement"},
+            "e2e": {"value": m / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(X.nbytes + Q.nbytes),
+                    "d2h_bytes_per_step": int(m * k * 8)},
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -373,17 +549,24 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--mode", default="fp32", choices=["fp32", "bf16", "fp8"])
+    ap.add_argument("--mode", default=HEADLINE_MODE, choices=["fp32", "bf16", "fp8"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"],
+                    help="c2 = the headline allknn workload; c1 / c3 = the suite's other searchbatch workloads")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--n", type=int, default=N_DB,
+    ap.add_argument("--cpu-queries", type=int, default=64, help="c1/c3: queries timed on the CPU")
+    ap.add_argument("--n", type=int, default=None,
                     help="database size (profiling captures use a smaller case of the same workload)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true", help="omit the plain FP32 comparison run")
     ap.add_argument("--overfetch", type=float, default=None,
                     help="candidates per neighbour kept by the reduced-precision scan")
     args = ap.parse_args()
-    N_DB = args.n
+    if args.n is not None and args.workload == "c2":
+        N_DB = args.n
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload != "c2":
+        workload_arm(args)
     else:
         gpu_arm(args)
 
