@@ -71,6 +71,9 @@ struct ssg_index {
     // BF16 tensor-core mode: operand tiles of the database and the queries,
     // per-row norms of the padded database, and the device status word.
     DevBuf tc_db, tc_norm, tc_q, status;
+    // K-streaming tensor-core path (FP8 mode, and BF16 for dim > 256): operand
+    // tiles, per-row FP8 scales, per-row epilogue coefficients, query tiles
+    DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
     // plain FP32 GEMM-form path: |x|^2 per row and its maximum, query flags of
     // the completeness check and the fallback's buffers
     DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand;
@@ -199,6 +202,35 @@ int build_tc_tiles(ssg_index *idx) {
     return SSG_OK;
 }
 
+// The resident-query BF16 kernel holds a query tile on chip (dim <= 256);
+// FP8 and wider BF16 stream both operands along K.
+bool uses_stream(const ssg_index *idx) {
+    return idx->prec == SSG_PREC_FP8 || (idx->prec == SSG_PREC_BF16 && ssg::tc_padded_k(idx->dim) > 256);
+}
+
+// (Re)builds the K-block operand tiles, FP8 scales and epilogue coefficients.
+int build_stream_tiles(ssg_index *idx) {
+    const int fp8 = idx->prec == SSG_PREC_FP8;
+    const int64_t tiles = ssg::tc_tiles(idx->n);
+    SSG_CK(idx->st_db.ensure(size_t(tiles) * ssg::stream_tile_bytes(idx->dim, fp8)), "allocating operand tiles");
+    float *scale = nullptr;
+    if (fp8) {
+        SSG_CK(idx->st_scale.ensure(size_t(tiles) * 128 * 4), "allocating FP8 scales");
+        scale = static_cast<float *>(idx->st_scale.p);
+    }
+    SSG_CK(ssg::launch_stream_tiles(static_cast<const float *>(idx->db.p), idx->n, idx->dim, fp8, tiles,
+                                    static_cast<uint8_t *>(idx->st_db.p), scale, idx->stream, &idx->last_launches),
+           "building operand tiles");
+    SSG_CK(idx->st_alpha.ensure(size_t(tiles) * 128 * 4), "allocating epilogue coefficients");
+    SSG_CK(idx->st_beta.ensure(size_t(tiles) * 128 * 4), "allocating epilogue coefficients");
+    SSG_CK(ssg::launch_stream_coefs(idx->metric, static_cast<const float *>(idx->db.p), idx->n, idx->dim, tiles * 128,
+                                    scale, static_cast<float *>(idx->st_alpha.p), static_cast<float *>(idx->st_beta.p),
+                                    idx->stream, &idx->last_launches),
+           "computing epilogue coefficients");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building operand tiles");
+    return SSG_OK;
+}
+
 int add_rows(ssg_index *idx, const void *src, int64_t rows, int64_t ld, bool src_device) {
     int rc = ensure_db_capacity(idx, idx->n + rows);
     if (rc) return rc;
@@ -227,8 +259,8 @@ int add_rows(ssg_index *idx, const void *src, int64_t rows, int64_t ld, bool src
                "reading the norm maximum");
         SSG_CK(cudaStreamSynchronize(idx->stream), "computing squared norms");
     }
-    if (idx->prec == SSG_PREC_BF16) {
-        rc = build_tc_tiles(idx);
+    if (idx->prec != SSG_PREC_FP32) {
+        rc = uses_stream(idx) ? build_stream_tiles(idx) : build_tc_tiles(idx);
         if (rc) return rc;
     }
     return SSG_OK;
@@ -249,13 +281,10 @@ int validate_create(int metric, int elem, int64_t dim, int64_t n, int64_t ld, in
     if (n < 0 || n >= (int64_t(1) << 32) - 1)
         return fail(nullptr, SSG_EINVAL, "database length %lld out of range", (long long)n);
     if (ld < dim) return fail(nullptr, SSG_EINVAL, "leading dimension %lld < dim %lld", (long long)ld, (long long)dim);
-    if (prec != SSG_PREC_FP32 && prec != SSG_PREC_BF16)
+    if (prec != SSG_PREC_FP32 && prec != SSG_PREC_BF16 && prec != SSG_PREC_FP8)
         return fail(nullptr, SSG_EUNSUPPORTED, "precision mode %d is not available in this build", prec);
     if (prec != SSG_PREC_FP32 && metric == SSG_METRIC_HAMMING)
         return fail(nullptr, SSG_EUNSUPPORTED, "Hamming distances are integers: only the exact mode exists");
-    if (prec == SSG_PREC_BF16 && ssg::tc_padded_k(dim) > 256)
-        return fail(nullptr, SSG_EUNSUPPORTED, "the BF16 mode keeps query tiles on chip: dim <= 256 (got %lld)",
-                    (long long)dim);
     return SSG_OK;
 }
 
@@ -514,13 +543,17 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
 
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db);
+int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                   uint32_t *d_ids, float *d_dists, bool queries_are_db);
 
 // Dispatch: BF16 tensor-core mode, Hamming, or the plain FP32 method (GEMM
 // form when its heaps fit, otherwise the exact direct scan).
 int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
             uint32_t *d_ids, float *d_dists, bool queries_are_db = false) {
-    if (idx->prec == SSG_PREC_BF16)
+    if (idx->prec != SSG_PREC_FP32) {
+        if (uses_stream(idx)) return run_knn_stream(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
         return run_knn_tc(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
+    }
     idx->last_fallbacks = 0;
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
         const int take = k + (exclude_self ? 1 : 0);
@@ -615,6 +648,90 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     SSG_CK(cudaStreamSynchronize(idx->stream), "running the BF16 search");
     if (status != 0)
         return fail(idx, SSG_ETIMEOUT, "a bounded wait in the BF16 scan kernel gave up (code %d)", status);
+    return SSG_OK;
+}
+
+// The K-streaming pipeline (FP8, or BF16 for wide vectors): operand tiles
+// of the queries (the database's own for allknn), the tcgen05 scan keeping
+// kk = overfetch * k approximate candidates per query and split, then the
+// exact FP32 rerank + (distance, id) merge.
+int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                   uint32_t *d_ids, float *d_dists, bool queries_are_db) {
+    const int fp8 = idx->prec == SSG_PREC_FP8;
+    const int take = k + (exclude_self ? 1 : 0);
+    int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
+    kk64 = std::max<int64_t>(kk64, take);
+    kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
+    int kk = int(kk64);
+    int cs = 0, stages = 0;
+    while (kk > take && !ssg::stream_choose(kk, &cs, &stages)) --kk;
+    if (!ssg::stream_choose(kk, &cs, &stages))
+        return fail(idx, SSG_EUNSUPPORTED, "k = %d does not fit the tensor-core kernel's on-chip top-k", take);
+    const int64_t qtiles = (m + 127) / 128;
+    const int64_t n_tiles = ssg::tc_tiles(idx->n);
+    int64_t splits = idx->splits_param > 0 ? idx->splits_param
+                                           : (ssg::device_sm_count() + qtiles - 1) / qtiles;
+    splits = std::min<int64_t>(splits, n_tiles);
+    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / (kk * cs)));
+    splits = std::max<int64_t>(1, splits);
+    const int segs = int(splits) * cs;
+    const size_t per_query = size_t(segs) * kk * 8;
+    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
+    chunk = std::min<int64_t>(chunk, qtiles * 128);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    const size_t tb = ssg::stream_tile_bytes(idx->dim, fp8);
+    const uint8_t *qt = static_cast<const uint8_t *>(idx->st_db.p);
+    const float *qgamma = fp8 ? static_cast<const float *>(idx->st_scale.p) : nullptr;
+    if (!queries_are_db) {
+        SSG_CK(idx->st_q.ensure(size_t(qtiles) * tb), "allocating query tiles");
+        float *qs = nullptr;
+        if (fp8) {
+            SSG_CK(idx->st_qscale.ensure(size_t(qtiles) * 128 * 4), "allocating query scales");
+            qs = static_cast<float *>(idx->st_qscale.p);
+        }
+        SSG_CK(ssg::launch_stream_tiles(static_cast<const float *>(dq), m, idx->dim, fp8, qtiles,
+                                        static_cast<uint8_t *>(idx->st_q.p), qs, idx->stream, &idx->last_launches),
+               "building query tiles");
+        qt = static_cast<const uint8_t *>(idx->st_q.p);
+        qgamma = qs;
+    }
+    ScanTimer timer(idx);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        SSG_RC(timer.begin());
+        SSG_CK(ssg::launch_stream_scan(qt + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->st_db.p),
+                                       static_cast<const float *>(idx->st_alpha.p),
+                                       static_cast<const float *>(idx->st_beta.p), qgamma ? qgamma + c0 : nullptr,
+                                       idx->n, mc, idx->dim, fp8, kk, int(splits),
+                                       static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
+                                       idx->stream, &idx->last_launches, nullptr),
+               "launching the tensor-core scan kernel");
+        SSG_RC(timer.end());
+        ssg::FinalizeArgs f{};
+        f.cand = static_cast<const uint64_t *>(idx->cand.p);
+        f.segs = segs;
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim,
+                                           static_cast<const float *>(dq) + size_t(c0) * idx->dim,
+                                           dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches),
+               "launching the rerank kernel");
+        SSG_RC(timer.collect());
+    }
+    int status = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the tensor-core search");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the tensor-core scan kernel gave up (code %d)", status);
     return SSG_OK;
 }
 
@@ -901,6 +1018,8 @@ void ssg_destroy(ssg_index *idx) {
     idx->tc_norm.release();
     idx->tc_q.release();
     idx->status.release();
+    for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale})
+        b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand})
         b->release();

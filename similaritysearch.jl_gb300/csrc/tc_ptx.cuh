@@ -116,6 +116,18 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64
         : "memory");
 }
 
+// D[tmem] (+)= A * B^T, kind::f8f6f4 (FP8 / FP6 / FP4 in, FP32 acc); the
+// operand formats are in the instruction descriptor.
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrives once on `bar` when every tcgen05 async op issued so far by this
 // thread has completed.
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
@@ -178,6 +190,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4)                      // D format: F32
            | (1u << 7)                    // A format: BF16
            | (1u << 10)                   // B format: BF16
+           | (uint32_t(N >> 3) << 17)     // N >> 3
+           | (uint32_t(M >> 4) << 24);    // M >> 4
+}
+
+// Instruction descriptor: kind::f8f6f4 with E4M3 A/B (format code 0), FP32
+// accumulator, both operands K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N) {
+    return (1u << 4)                      // D format: F32
            | (uint32_t(N >> 3) << 17)     // N >> 3
            | (uint32_t(M >> 4) << 24);    // M >> 4
 }

@@ -1,0 +1,397 @@
+// tc_stream.cu -- tensor-core distance tiles for wide vectors, BF16 or FP8.
+//
+// The reduced-precision methods for any dimension: like tc_bf16.cu, but both
+// operands stream through shared memory one K-block at a time, so a 768-wide
+// query tile does not have to stay on chip.  Operands are BF16 or FP8 e4m3
+// with one scale per vector (x ~= s_x * x8, s_x = max|x_i| / 448); the
+// tensor cores accumulate in FP32 (tcgen05.mma kind::f16 / kind::f8f6f4) and
+// the epilogue turns the raw dot v into an approximate distance
+//      d~ = fma(v * gamma_q, alpha_x, beta_x)
+// with per-query gamma (the query's scale) and per-row alpha / beta:
+//      IP, NormCosine:  alpha = -s_x,              beta = 0
+//      Cosine:          alpha = -s_x / |x|,        beta = 0
+//      SqL2, L2:        alpha = -2 s_x,            beta = |x|^2
+// which ranks like the exact metric.  kk = overfetch * k candidates per query
+// survive into the exact FP32 rerank (finalize_rerank_kernel).
+//
+// Layout in HBM: tiles of 128 rows; each tile is a sequence of K-blocks of
+// 128 bytes per row (64 BF16 or 128 FP8 elements) with the 128-byte swizzle
+// applied, so one K-block of a query tile and one of a database tile (16 KB
+// each) form one pipeline stage, fetched with two TMA bulk copies.
+//
+// Roles per CTA (one 128-query tile): warp 0 TMA producer, warp 1 TMEM owner
+// and MMA issuer (double-buffered 128 x 128 FP32 accumulators), 4 * CS
+// epilogue warps (CS warps share each TMEM lane quarter and split the
+// columns).  Every wait is bounded (tc_ptx.cuh).
+#include "common.cuh"
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+
+namespace ssg {
+
+namespace {
+
+constexpr int TILE = 128;
+constexpr int SWB = 128;                      // bytes per swizzled K-block row
+constexpr int KBLOCK_BYTES = TILE * SWB;      // 16 KB per operand per K-block
+constexpr int kBufCap = 12;
+constexpr int kDrainTrigger = 4;
+constexpr int kDrainEvery = 8;
+
+template <int CS>
+__host__ __device__ constexpr int st_threads() { return 64 + TILE * CS; }
+
+// ---------------------------------------------------------------------------
+// Prep: rows -> swizzled K-block tiles (BF16 or scaled FP8) + per-row scale.
+// One warp per row.
+// ---------------------------------------------------------------------------
+__global__ void stream_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kbytes, int fp8,
+                                   int64_t tiles, uint8_t *__restrict__ out, float *__restrict__ scale) {
+    const int lane = threadIdx.x % 32;
+    const int64_t wid = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+    const int64_t nw = int64_t(gridDim.x) * blockDim.x / 32;
+    const int es = fp8 ? 1 : 2;
+    const int per_chunk = 16 / es;             // elements per 16-byte chunk
+    const int nchunks = kbytes / 16;           // chunks per padded row
+    const size_t tile_bytes = size_t(TILE) * kbytes;
+    for (int64_t row = wid; row < tiles * TILE; row += nw) {
+        const bool valid = row < rows;
+        const float *xr = x + (valid ? row : 0) * dim;
+        float s = 1.0f;
+        if (fp8) {
+            float mx = 0.0f;
+            if (valid)
+                for (int c = lane; c < dim; c += 32) mx = fmaxf(mx, fabsf(xr[c]));
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            s = mx > 0.0f ? mx / 448.0f : 1.0f;
+            if (lane == 0) scale[row] = valid ? s : 0.0f;
+        }
+        const float inv = 1.0f / s;
+        const int64_t tile = row / TILE;
+        const int r = int(row % TILE);
+        for (int ch = lane; ch < nchunks; ch += 32) {
+            __align__(16) uint8_t buf[16];
+            const int e0 = ch * per_chunk;
+            if (fp8) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const float f = (valid && e0 + e < dim) ? xr[e0 + e] * inv : 0.0f;
+                    buf[e] = __nv_cvt_float_to_fp8(f, __NV_SATFINITE, __NV_E4M3);
+                }
+            } else {
+                __nv_bfloat16 *b = reinterpret_cast<__nv_bfloat16 *>(buf);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) b[e] = __float2bfloat16_rn((valid && e0 + e < dim) ? xr[e0 + e] : 0.0f);
+            }
+            const int kb = ch / (SWB / 16);
+            const uint32_t off = tc::swizzled_offset(uint32_t(r), uint32_t((ch % (SWB / 16)) * 16), SWB);
+            uint8_t *dst = out + size_t(tile) * tile_bytes + size_t(kb) * KBLOCK_BYTES + off;
+            *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(buf);
+        }
+    }
+}
+
+// alpha / beta per padded database row (see the file comment)
+__global__ void stream_coef_kernel(const float *__restrict__ x, int64_t rows, int dim, int64_t padded, int metric,
+                                   const float *__restrict__ scale, float *__restrict__ alpha,
+                                   float *__restrict__ beta) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= padded) return;
+    if (i >= rows) { alpha[i] = 0.0f; beta[i] = 0.0f; return; }
+    const float s = scale ? scale[i] : 1.0f;
+    float sq = 0.0f;
+    if (metric == SQL2 || metric == L2 || metric == COSINE) {
+        const float *r = x + i * dim;
+        for (int c = 0; c < dim; ++c) sq = fmaf(r[c], r[c], sq);
+    }
+    if (metric == SQL2 || metric == L2) { alpha[i] = -2.0f * s; beta[i] = sq; }
+    else if (metric == COSINE) { alpha[i] = sq > 0.0f ? -s / sqrtf(sq) : 0.0f; beta[i] = 0.0f; }
+    else { alpha[i] = -s; beta[i] = 0.0f; }
+}
+
+struct StreamArgs {
+    const uint8_t *qt, *dt;        // query / database K-block tiles
+    const float *alpha, *beta;     // per padded database row
+    const float *qgamma;           // per query (FP8 scale) or nullptr (1)
+    int64_t n, m;
+    int kblocks;                   // K-blocks per tile
+    int fp8;
+    int kk, splits;
+    int64_t split_tiles, n_tiles;
+    uint64_t *cand;
+    int *err;
+};
+
+template <int CS, int STAGES>
+struct StreamSmem {
+    static size_t heap_bytes(int kk) { return size_t(TILE) * CS * (kk + kBufCap) * 8; }
+    static size_t total(int kk) { return 1024 + size_t(STAGES) * 2 * KBLOCK_BYTES + heap_bytes(kk) + 256; }
+};
+
+template <int CS, int STAGES>
+__global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *sAB = smem;  // [STAGES][A | B]
+    uint64_t *heap_base = reinterpret_cast<uint64_t *>(sAB + size_t(STAGES) * 2 * KBLOCK_BYTES);
+    uint64_t *buf_base = heap_base + size_t(TILE) * CS * a.kk;
+    uint64_t *bars = buf_base + size_t(TILE) * CS * kBufCap;
+    uint64_t *full = bars;
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *mma_done = acc_empty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+
+    constexpr int NCOLS = 2 * TILE;
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 4 * CS);
+        }
+        tc::mbar_init(mma_done, 1);
+        tc::fence_mbarrier_init();
+    }
+    if (warp == 1) tc::tmem_alloc<NCOLS>(tmem_slot);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    const int64_t t_lo = int64_t(blockIdx.y) * a.split_tiles;
+    int64_t t_hi = t_lo + a.split_tiles;
+    if (t_hi > a.n_tiles) t_hi = a.n_tiles;
+    const int T_tiles = t_hi > t_lo ? int(t_hi - t_lo) : 0;
+    const int KB = a.kblocks;
+    const size_t tile_bytes = size_t(KB) * KBLOCK_BYTES;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint8_t *qtile = a.qt + size_t(blockIdx.x) * tile_bytes;
+            int it = 0;
+            bool ok = true;
+            for (int t = 0; ok && t < T_tiles; ++t) {
+                const uint8_t *dtile = a.dt + size_t(t_lo + t) * tile_bytes;
+                for (int kb = 0; kb < KB; ++kb, ++it) {
+                    const int s = it % STAGES;
+                    if (!tc::mbar_wait(&empty[s], ((it / STAGES) & 1) ^ 1, a.err, 11)) { ok = false; break; }
+                    tc::mbar_arrive_expect_tx(&full[s], 2 * KBLOCK_BYTES);
+                    uint8_t *dst = sAB + size_t(s) * 2 * KBLOCK_BYTES;
+                    tc::bulk_g2s(dst, qtile + size_t(kb) * KBLOCK_BYTES, KBLOCK_BYTES, &full[s]);
+                    tc::bulk_g2s(dst + KBLOCK_BYTES, dtile + size_t(kb) * KBLOCK_BYTES, KBLOCK_BYTES, &full[s]);
+                }
+            }
+            // wait (bounded) for the copies of the last stages issued
+            for (int j = it - STAGES < 0 ? 0 : it - STAGES; j < it; ++j)
+                tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, a.err, 12);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = a.fp8 ? tc::idesc_e4m3_f32(TILE, TILE) : tc::idesc_bf16_f32(TILE, TILE);
+            const uint32_t base = tc::smem_u32(sAB);
+            int it = 0;
+            bool ok = true;
+            for (int t = 0; ok && t < T_tiles; ++t) {
+                const int b = t & 1;
+                if (!tc::mbar_wait(&acc_empty[b], ((t >> 1) & 1) ^ 1, a.err, 13)) break;
+                tc::tc_fence_after();
+                const uint32_t d_tmem = tmem_base + uint32_t(b * TILE);
+                for (int kb = 0; kb < KB; ++kb, ++it) {
+                    const int s = it % STAGES;
+                    if (!tc::mbar_wait(&full[s], (it / STAGES) & 1, a.err, 14)) { ok = false; break; }
+                    tc::tc_fence_after();
+                    const uint32_t sa = base + uint32_t(s) * 2 * KBLOCK_BYTES;
+                    const uint32_t sb = sa + KBLOCK_BYTES;
+#pragma unroll
+                    for (int k = 0; k < SWB / 32; ++k) {  // 32 bytes of K per MMA
+                        const uint64_t ad = tc::smem_desc(sa + k * 32, SWB);
+                        const uint64_t bd = tc::smem_desc(sb + k * 32, SWB);
+                        if (a.fp8) tc::mma_f8(d_tmem, ad, bd, idesc, (kb | k) ? 1u : 0u);
+                        else tc::mma_f16(d_tmem, ad, bd, idesc, (kb | k) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                tc::mma_commit(&acc_full[b]);
+            }
+            tc::mma_commit(mma_done);
+            tc::mbar_wait(mma_done, 0, a.err, 15);
+        }
+        __syncwarp();
+    } else {
+        const int e = warp - 2;
+        const int cs = e / 4;
+        const int quarter = warp % 4;
+        const int row = quarter * 32 + lane;
+        const int64_t query = int64_t(blockIdx.x) * TILE + row;
+        constexpr int hs = TILE * CS;
+        constexpr int CHUNKS = TILE / 32 / CS;
+        const float gamma = (a.qgamma && query < a.m) ? a.qgamma[query] : 1.0f;
+        uint64_t *heap = heap_base + (e * 32 + lane);
+        uint64_t *cbuf = buf_base + (e * 32 + lane);
+        Heap{heap, a.kk, hs}.init();
+        uint64_t top = KEY_EMPTY;
+        float topd = INFINITY;
+        int nbuf = 0;
+        for (int t = 0; t < T_tiles; ++t) {
+            const int b = t & 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 16) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            tc::tc_fence_after();
+            const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
+            uint32_t r[CHUNKS][32];
+            __syncwarp();
+            const uint32_t tbase =
+                tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * TILE + cs * (TILE / CS));
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) tc::tmem_ld_32x32b_x32_async(tbase + uint32_t(c * 32), r[c]);
+            tc::tmem_wait_ld();
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) {
+                const int64_t id0 = row0 + c * 32;
+                const float *al = a.alpha + id0;
+                const float *be = a.beta + id0;
+                float dv[32];
+                float gmin[4];
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    float mn = INFINITY;
+#pragma unroll
+                    for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                        dv[j] = fmaf(__uint_as_float(r[c][j]) * gamma, __ldg(al + j), __ldg(be + j));
+                        mn = fminf(mn, dv[j]);
+                    }
+                    gmin[g] = mn;
+                }
+                const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+                if (__any_sync(0xffffffffu, dmin <= topd)) {
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        if (!__any_sync(0xffffffffu, gmin[g] <= topd)) continue;
+#pragma unroll
+                        for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                            cbuf[nbuf * hs] = make_key(dv[j], uint32_t(id0 + j));
+                            nbuf += (dv[j] <= topd && id0 + j < a.n) ? 1 : 0;
+                        }
+                        if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
+                            top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+                            nbuf = 0;
+                            topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                        }
+                    }
+                }
+            }
+        }
+        top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        Heap H{heap, a.kk, hs};
+        if (query < a.m) {
+            H.sort_ascending();
+            uint64_t *out = a.cand + ((size_t(query) * a.splits + blockIdx.y) * CS + cs) * a.kk;
+            for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc<NCOLS>(tmem_base);
+    }
+}
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+template <int CS, int STAGES>
+cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st) {
+    const size_t smem = StreamSmem<CS, STAGES>::total(a.kk);
+    auto kern = tc_stream_kernel<CS, STAGES>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((a.m + TILE - 1) / TILE), unsigned(a.splits));
+    kern<<<grid, st_threads<CS>(), smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int stream_kbytes(int64_t dim, int fp8) {
+    const int64_t bytes = dim * (fp8 ? 1 : 2);
+    return int((bytes + SWB - 1) / SWB * SWB);
+}
+size_t stream_tile_bytes(int64_t dim, int fp8) { return size_t(TILE) * stream_kbytes(dim, fp8); }
+
+// (column splits, stages) for kk candidates, or false.
+bool stream_choose(int kk, int *cs, int *stages) {
+    if (StreamSmem<2, 4>::total(kk) <= kMaxSmem) { *cs = 2; *stages = 4; return true; }
+    if (StreamSmem<2, 3>::total(kk) <= kMaxSmem) { *cs = 2; *stages = 3; return true; }
+    if (StreamSmem<1, 4>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 4; return true; }
+    if (StreamSmem<1, 3>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 3; return true; }
+    if (StreamSmem<1, 2>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 2; return true; }
+    return false;
+}
+
+cudaError_t launch_stream_tiles(const float *x, int64_t rows, int64_t dim, int fp8, int64_t tiles, uint8_t *out,
+                                float *scale, cudaStream_t st, int *launches) {
+    const int64_t warps = tiles * TILE;
+    int64_t blocks = (warps * 32 + 255) / 256;
+    if (blocks > 148 * 32) blocks = 148 * 32;
+    if (blocks < 1) blocks = 1;
+    if (launches) *launches += 1;
+    stream_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), stream_kbytes(dim, fp8), fp8, tiles,
+                                                          out, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded,
+                                const float *scale, float *alpha, float *beta, cudaStream_t st, int *launches) {
+    if (launches) *launches += 1;
+    stream_coef_kernel<<<unsigned((padded + 255) / 256), 256, 0, st>>>(x, rows, int(dim), padded, metric, scale,
+                                                                       alpha, beta);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, const float *alpha, const float *beta,
+                               const float *qgamma, int64_t n, int64_t m, int64_t dim, int fp8, int kk, int splits,
+                               uint64_t *cand, int *err, cudaStream_t st, int *launches, int *segs_per_split) {
+    StreamArgs a{};
+    a.qt = q_tiles;
+    a.dt = d_tiles;
+    a.alpha = alpha;
+    a.beta = beta;
+    a.qgamma = qgamma;
+    a.n = n;
+    a.m = m;
+    a.kblocks = stream_kbytes(dim, fp8) / SWB;
+    a.fp8 = fp8;
+    a.kk = kk;
+    a.splits = splits;
+    a.n_tiles = (n + TILE - 1) / TILE;
+    a.split_tiles = (a.n_tiles + splits - 1) / splits;
+    a.cand = cand;
+    a.err = err;
+    int cs = 0, stages = 0;
+    if (!stream_choose(kk, &cs, &stages)) return cudaErrorInvalidValue;
+    if (segs_per_split) *segs_per_split = cs;
+    if (launches) *launches += 1;
+    if (cs == 2) return stages == 4 ? launch_stream_t<2, 4>(a, st) : launch_stream_t<2, 3>(a, st);
+    if (stages == 4) return launch_stream_t<1, 4>(a, st);
+    if (stages == 3) return launch_stream_t<1, 3>(a, st);
+    return launch_stream_t<1, 2>(a, st);
+}
+
+}  // namespace ssg

@@ -118,10 +118,8 @@ def test_bf16_allknn_exclude_self(ss):
     assert O.macrorecall(gold, gi[rows]) >= 0.99
 
 
-def test_bf16_rejects_hamming_and_large_dim(ss):
+def test_bf16_rejects_hamming(ss):
+    # Hamming distances are integers: only the exact method exists for them
     B = np.zeros((10, 2), dtype=np.uint64)
     with pytest.raises(ss._native.UnsupportedError):
         ss.GPUExhaustiveSearch(ss.Dist.Bits.Hamming(), ss.MatrixDatabase.from_rows(B), precision="bf16")
-    X = np.zeros((10, 300), dtype=np.float32)
-    with pytest.raises(ss._native.UnsupportedError):
-        ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X), precision="bf16")
