@@ -542,6 +542,126 @@ def workload_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def make_c4(n=2_000_000, d=768, batches=200):
+    """C4: 4,096-cluster mixture (sigma U[0.05, 0.3]) with log-normal(0, 0.25)
+    norms; batch sizes round(LogNormal(ln 64, 1)) clipped to [1, 4096]; k
+    uniform over {1, 10, 100}; queries drawn from the same mixture."""
+    centres = np.random.default_rng(9).standard_normal((4096, d), dtype=np.float32)
+    sig = np.random.default_rng(10).uniform(0.05, 0.3, size=4096).astype(np.float32)
+
+    def draw(count, seed_lab, seed_norm):
+        g = np.random.default_rng(seed_lab)
+        out = np.empty((count, d), dtype=np.float32)
+        for s0 in range(0, count, 250_000):
+            c = min(250_000, count - s0)
+            lab = g.integers(0, 4096, size=c)
+            blk = g.standard_normal((c, d), dtype=np.float32)
+            blk *= sig[lab, None]
+            blk += centres[lab]
+            blk /= np.linalg.norm(blk, axis=1, keepdims=True)
+            out[s0:s0 + c] = blk
+        out *= np.random.default_rng(seed_norm).lognormal(0.0, 0.25, size=(count, 1)).astype(np.float32)
+        return out
+
+    X = draw(n, 11, 12)
+    sizes = np.clip(np.round(np.random.default_rng(13).lognormal(np.log(64), 1.0, size=batches)), 1, 4096)
+    sizes = sizes.astype(np.int64)
+    ks = np.random.default_rng(14).choice([1, 10, 100], size=batches)
+    Q = draw(int(sizes.sum()), 15, 16)
+    return X, Q, sizes, ks
+
+
+def c4_arm(args):
+    cx = Ctx()
+    torch, N, L = cx.torch, cx.N, cx.L
+    from oracle import oracle as O
+    X, Q, sizes, ks = make_c4(args.n if args.n is not None else 2_000_000, batches=args.batches)
+    n, d = X.shape
+    mode = args.mode if args.mode != "bf16" else "fp8"
+    metric = N.METRIC_IP
+    h = C.c_void_p()
+    N.check(L.ssg_create(metric, N.ELEM_F32, d, n, X.ctypes.data_as(C.c_void_p), d, PREC[mode], C.byref(h)))
+    N.check(L.ssg_set_stream(h, C.c_void_p(torch.cuda.current_stream().cuda_stream)), h)
+    Qd = torch.from_numpy(Q).cuda()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    kmax = int(ks.max())
+    ids_d = torch.empty((int(sizes.max()), kmax), dtype=torch.int32, device="cuda")
+    dd_d = torch.empty((int(sizes.max()), kmax), dtype=torch.float32, device="cuda")
+
+    def run_stream(plain):
+        N.check(L.ssg_set_param(h, b"plain", 1.0 if plain else 0.0), h)
+        lat, results = [], []
+        for b in range(len(sizes)):
+            m, k = int(sizes[b]), int(ks[b])
+            q = C.c_void_p(Qd.data_ptr() + int(offs[b]) * d * 4)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            N.check(L.ssg_search_device(h, q, m, k, C.c_void_p(ids_d.data_ptr()), C.c_void_p(dd_d.data_ptr()), 0), h)
+            torch.cuda.synchronize()
+            lat.append(time.perf_counter() - t0)
+            # the call writes m rows of k contiguously
+            results.append(ids_d.view(-1)[:m * k].view(m, k).cpu().numpy().view(np.uint32).copy())
+        return np.array(lat), results
+
+    # over-fetch picked by the autotuner: smallest with recall@10 >= 0.99 on a
+    # calibration sample against the plain method on the same index
+    nc = min(2048, Q.shape[0])
+    calib = Qd[:nc].contiguous()
+    ci = torch.empty((nc, 10), dtype=torch.int32, device="cuda")
+    cd = torch.empty((nc, 10), dtype=torch.float32, device="cuda")
+    N.check(L.ssg_set_param(h, b"plain", 1.0), h)
+    N.check(L.ssg_search_device(h, C.c_void_p(calib.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
+                                C.c_void_p(cd.data_ptr()), 0), h)
+    gold_c = ci.cpu().numpy().view(np.uint32).copy()
+    N.check(L.ssg_set_param(h, b"plain", 0.0), h)
+    chosen = None
+    for c in (1.0, 1.25, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0):
+        N.check(L.ssg_set_param(h, b"overfetch", c), h)
+        N.check(L.ssg_search_device(h, C.c_void_p(calib.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
+                                    C.c_void_p(cd.data_ptr()), 0), h)
+        if O.macrorecall(gold_c, ci.cpu().numpy().view(np.uint32)) >= 0.997:
+            chosen = c
+            break
+    chosen = chosen or 16.0
+    N.check(L.ssg_set_param(h, b"overfetch", chosen), h)
+    run_stream(False)  # warm-up pass
+    with ClockSampler(cx.local) as clk:
+        lat_r, res_r = run_stream(False)
+    lat_p, res_p = run_stream(True)
+    # recall@10 of the reduced method against the plain method (k >= 10 batches)
+    rec, cnt = 0.0, 0
+    for b in range(len(sizes)):
+        if ks[b] >= 10:
+            rec += O.macrorecall(res_p[b][:, :10], res_r[b][:, :10]) * sizes[b]
+            cnt += sizes[b]
+    rec = rec / max(1, cnt)
+    # FP64 oracle on a few queries of the first k>=10 batch
+    b0 = int(np.nonzero(ks >= 10)[0][0])
+    bq = np.nonzero((ks >= 10) & (sizes >= 8))[0]
+    b0 = int(bq[0]) if bq.size else b0
+    qs = Q[offs[b0]:offs[b0] + min(8, sizes[b0])]
+    fi, _ = O.searchbatch_f64("ip", X, qs, 10, nthreads=os.cpu_count() or 1)
+    r64_red = O.macrorecall(fi, res_r[b0][:qs.shape[0], :10])
+    r64_pl = O.macrorecall(fi, res_p[b0][:qs.shape[0], :10])
+    L.ssg_destroy(h)
+    tq = int(sizes.sum())
+    line = {"metric": "queries/s (c4 batched stream)", "value": tq / lat_r.sum(), "unit": "queries/s",
+            "n_gpus": cx.world, "batches": int(len(sizes)), "higher_is_better": True, "vs_baseline": None,
+            "dtype": mode, "data": "synthetic, seeded 4096-cluster mixture, log-normal norms",
+            "config": {"workload": f"IP request stream, n={n:,}, d={d}, {len(sizes)} batches "
+                                   f"(sizes LogNormal(ln 64,1) in [1,4096], k in {{1,10,100}})",
+                       "mode": mode, "overfetch_autotuned": chosen,
+                       "batching": "one search call per batch (no CUDA-graph / persistent kernel yet)"},
+            "latency_ms": {"p50": float(np.percentile(lat_r, 50) * 1e3), "p99": float(np.percentile(lat_r, 99) * 1e3)},
+            "recall@10_vs_plain": rec, "recall@10_vs_fp64_sample": {"reduced": r64_red, "plain": r64_pl,
+                                                                    "queries": int(qs.shape[0])},
+            "plain_fp32": {"value": tq / lat_p.sum(),
+                           "latency_ms": {"p50": float(np.percentile(lat_p, 50) * 1e3),
+                                          "p99": float(np.percentile(lat_p, 99) * 1e3)}},
+            "speedup_vs_plain": float(lat_p.sum() / lat_r.sum()), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_DB
     ap = argparse.ArgumentParser()
@@ -550,10 +670,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--mode", default=HEADLINE_MODE, choices=["fp32", "bf16", "fp8"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"],
                     help="c2 = the headline allknn workload; c1 / c3 = the suite's other searchbatch workloads")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--cpu-queries", type=int, default=64, help="c1/c3: queries timed on the CPU")
+    ap.add_argument("--batches", type=int, default=200, help="c4: batches in the request stream")
     ap.add_argument("--n", type=int, default=None,
                     help="database size (profiling captures use a smaller case of the same workload)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
@@ -565,6 +686,8 @@ def main():
         N_DB = args.n
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "c4":
+        c4_arm(args)
     elif args.workload != "c2":
         workload_arm(args)
     else:

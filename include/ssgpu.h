@@ -122,12 +122,17 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
                uint32_t *ids, float *dists);
 
 /* Tunables: "overfetch" (candidates per k in BF16/FP8 modes), "splits"
- * (database splits per query tile, 0 = auto), "profile" (1 = time the main
- * kernel with events), "max_cands".  Unknown keys return SSG_EINVAL. */
+ * (database splits per query tile, 0 = auto), "margin" (extra candidates of
+ * the plain GEMM-form scan, 0 = auto), "exact_scan" (1 = plain method through
+ * the direct difference-form scan only), "plain" (1 = plain FP32 method on a
+ * BF16/FP8 index, e.g. to calibrate "overfetch" against it), "profile"
+ * (1 = time the scan kernel with events).  Unknown keys return SSG_EINVAL. */
 int ssg_set_param(ssg_index *idx, const char *key, double value);
 /* Readable keys: the tunables plus "n", "dim", "metric", "precision",
  * "main_kernel_ms" / "main_kernel_launches" (accumulated while profiling),
- * "kernel_launches" (kernels launched by the last call), "device_bytes". */
+ * "kernel_launches" (kernels launched by the last call), "fallbacks" (queries
+ * the last plain call recomputed with the exact scan), "max_x_sq",
+ * "device_bytes". */
 int ssg_get_param(ssg_index *idx, const char *key, double *value);
 
 /* Runs the index's work on `stream` (a cudaStream_t) instead of its own. */

@@ -77,9 +77,11 @@ struct ssg_index {
     // plain FP32 GEMM-form path: |x|^2 per row and its maximum, query flags of
     // the completeness check and the fallback's buffers
     DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand;
+    DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
     float max_x_sq = 0.0f;
     int margin_param = 0;
     int exact_scan_param = 0;
+    int plain_param = 0;  // 1: run the plain FP32 method on a reduced-precision index
     int last_fallbacks = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -330,7 +332,6 @@ int choose_splits(ssg_index *idx, int64_t m, int kk, int qpb) {
     int64_t s = (target + qtiles - 1) / qtiles;
     const int64_t min_len = std::max<int64_t>(1024, int64_t(8) * kk);
     s = std::min<int64_t>(s, std::max<int64_t>(1, idx->n / min_len));
-    s = std::min<int64_t>(s, std::max<int64_t>(1, 8192 / kk));
     return int(std::max<int64_t>(1, s));
 }
 
@@ -363,6 +364,31 @@ struct ScanTimer {
         int _rc = (call);   \
         if (_rc) return _rc; \
     } while (0)
+
+// Reduces each query's `segs` sorted candidate segments (kk keys each) by
+// merge passes until one merge block holds them; returns the buffer and the
+// segment count the final merge should read.
+int reduce_segments(ssg_index *idx, const uint64_t *cand, int64_t m, int segs, int kk, const uint64_t **out,
+                    int *out_segs) {
+    const uint64_t *cur = cand;
+    int cs = segs;
+    int which = 0;
+    while (int64_t(cs) * kk > ssg::kMergeKeys) {
+        const int group = std::max(2, ssg::kMergeKeys / kk);
+        const int ns = (cs + group - 1) / group;
+        DevBuf &b = idx->red[which];
+        SSG_CK(b.ensure(size_t(m) * ns * kk * 8), "allocating merge scratch");
+        SSG_CK(ssg::launch_merge_groups(cur, m, cs, kk, group, static_cast<uint64_t *>(b.p), idx->stream,
+                                        &idx->last_launches),
+               "launching a merge pass");
+        cur = static_cast<const uint64_t *>(b.p);
+        cs = ns;
+        which ^= 1;
+    }
+    *out = cur;
+    *out_segs = cs;
+    return SSG_OK;
+}
 
 // The exact scan (direct FP32 or Hamming) then merge and decode.  dq are
 // device query rows (Float32 or UInt64), dqn their norms (Cosine).  self_ids
@@ -412,8 +438,7 @@ int run_exact_scan(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
         SSG_CK(e, "launching the scan kernel");
         SSG_RC(timer.end());
         ssg::FinalizeArgs f{};
-        f.cand = a.cand;
-        f.segs = splits;
+        SSG_RC(reduce_segments(idx, a.cand, mc, splits, kk, &f.cand, &f.segs));
         f.kk = kk;
         f.m = mc;
         f.k_out = k;
@@ -445,7 +470,6 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
                                            : (ssg::device_sm_count() + qtiles - 1) / qtiles;
     splits = std::min<int64_t>(splits, std::max<int64_t>(1, idx->n / 512));
-    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / kk));
     splits = std::max<int64_t>(1, splits);
     const int64_t split_len = (idx->n + splits - 1) / splits;
     const int segs = int(splits);
@@ -480,8 +504,7 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
                "launching the FP32 scan kernel");
         SSG_RC(timer.end());
         ssg::FinalizeArgs f{};
-        f.cand = a.cand;
-        f.segs = segs;
+        SSG_RC(reduce_segments(idx, a.cand, mc, segs, kk, &f.cand, &f.segs));
         f.kk = kk;
         f.m = mc;
         f.k_out = k;
@@ -550,7 +573,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
 // form when its heaps fit, otherwise the exact direct scan).
 int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
             uint32_t *d_ids, float *d_dists, bool queries_are_db = false) {
-    if (idx->prec != SSG_PREC_FP32) {
+    if (idx->prec != SSG_PREC_FP32 && !idx->plain_param) {
         if (uses_stream(idx)) return run_knn_stream(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
         return run_knn_tc(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
     }
@@ -587,7 +610,6 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
                                            : (ssg::device_sm_count() + qctas - 1) / qctas;
     splits = std::min<int64_t>(splits, n_tiles);
-    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / kk));
     splits = std::max<int64_t>(1, splits);
     // chunk the queries (a multiple of the CTA's query rows) to bound scratch
     const int segs = int(splits) * ssg::tc_segments_per_split(qt);
@@ -618,8 +640,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
                "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
-        f.cand = static_cast<const uint64_t *>(idx->cand.p);
-        f.segs = segs;
+        SSG_RC(reduce_segments(idx, static_cast<const uint64_t *>(idx->cand.p), mc, segs, kk, &f.cand, &f.segs));
         f.kk = kk;
         f.m = mc;
         f.k_out = k;
@@ -672,7 +693,6 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
                                            : (ssg::device_sm_count() + qtiles - 1) / qtiles;
     splits = std::min<int64_t>(splits, n_tiles);
-    splits = std::min<int64_t>(splits, std::max<int64_t>(1, 4096 / (kk * cs)));
     splits = std::max<int64_t>(1, splits);
     const int segs = int(splits) * cs;
     const size_t per_query = size_t(segs) * kk * 8;
@@ -710,8 +730,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
                "launching the tensor-core scan kernel");
         SSG_RC(timer.end());
         ssg::FinalizeArgs f{};
-        f.cand = static_cast<const uint64_t *>(idx->cand.p);
-        f.segs = segs;
+        SSG_RC(reduce_segments(idx, static_cast<const uint64_t *>(idx->cand.p), mc, segs, kk, &f.cand, &f.segs));
         f.kk = kk;
         f.m = mc;
         f.k_out = k;
@@ -946,6 +965,8 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->margin_param = int(value);
     } else if (k == "exact_scan") {
         idx->exact_scan_param = value != 0.0;
+    } else if (k == "plain") {
+        idx->plain_param = value != 0.0;
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -971,6 +992,7 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "kernel_launches") *value = idx->last_launches;
     else if (k == "margin") *value = idx->margin_param;
     else if (k == "exact_scan") *value = idx->exact_scan_param;
+    else if (k == "plain") *value = idx->plain_param;
     else if (k == "fallbacks") *value = idx->last_fallbacks;
     else if (k == "max_x_sq") *value = idx->max_x_sq;
     else if (k == "device_bytes")
@@ -1018,7 +1040,8 @@ void ssg_destroy(ssg_index *idx) {
     idx->tc_norm.release();
     idx->tc_q.release();
     idx->status.release();
-    for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale})
+    for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale,
+                      &idx->red[0], &idx->red[1]})
         b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand})

@@ -216,7 +216,39 @@ __global__ void finalize_kernel(FinalizeArgs a, int P) {
     }
 }
 
+// Merges groups of `group` sorted segments of kk keys into one sorted
+// segment of the group's kk smallest keys: the pass used when a query's
+// splits x kk candidates exceed one block's shared memory.
+__global__ void merge_groups_kernel(const uint64_t *__restrict__ in, int segs, int kk, int group, int out_segs,
+                                    int P, uint64_t *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *s = reinterpret_cast<uint64_t *>(smem);
+    const int64_t j = blockIdx.x;
+    const int g = blockIdx.y;
+    const int s0 = g * group;
+    const int ns = (segs - s0) < group ? (segs - s0) : group;
+    const int total = ns * kk;
+    const uint64_t *src = in + (size_t(j) * segs + s0) * kk;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < total ? src[i] : KEY_EMPTY;
+    block_bitonic_sort(s, P);
+    uint64_t *dst = out + (size_t(j) * out_segs + g) * kk;
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) dst[i] = s[i];
+}
+
 }  // namespace
+
+cudaError_t launch_merge_groups(const uint64_t *in, int64_t m, int segs, int kk, int group, uint64_t *out,
+                                cudaStream_t st, int *launches) {
+    const int out_segs = (segs + group - 1) / group;
+    const int P = next_pow2(int64_t(group) * kk);
+    const size_t smem = size_t(P) * 8;
+    cudaError_t e = cudaFuncSetAttribute(merge_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    if (launches) *launches += 1;
+    merge_groups_kernel<<<dim3(unsigned(m), unsigned(out_segs)), 256, smem, st>>>(in, segs, kk, group, out_segs, P,
+                                                                                  out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t st, int *launches) {
     const int P = next_pow2(int64_t(a.segs) * a.kk);

@@ -65,6 +65,13 @@ struct FinalizeArgs {
 };
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t st, int *launches);
 
+// Keys one merge block sorts at most (64 KB of shared memory).
+constexpr int kMergeKeys = 8192;
+// One reduction pass: each group of `group` sorted kk-key segments of every
+// query -> one sorted segment of its kk smallest keys (ceil(segs/group) out).
+cudaError_t launch_merge_groups(const uint64_t *in, int64_t m, int segs, int kk, int group, uint64_t *out,
+                                cudaStream_t st, int *launches);
+
 // Row norms: out[i] = sqrt(sum x^2) (COSINE) in sequential FMA order.
 cudaError_t launch_row_norms(const float *x, int64_t rows, int64_t dim, float *out,
                              cudaStream_t st, int *launches);

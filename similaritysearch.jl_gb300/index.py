@@ -128,6 +128,31 @@ class GPUExhaustiveSearch:
     def __len__(self):
         return int(self.get_param("n"))
 
+    def autotune_overfetch(self, Q, k: int, target_recall: float = 0.99,
+                           candidates=(1.0, 1.25, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0)) -> float:
+        """Picks the smallest over-fetch whose recall@k on the calibration
+        queries ``Q`` reaches ``target_recall`` against the plain FP32 method
+        on the same index (which matches ExhaustiveSearch), sets it and
+        returns it.  A no-op returning 1.0 for the plain method."""
+        if self.precision == "fp32":
+            return 1.0
+        ctx = GenericContext(logger=None)
+        self.set_param("plain", 1)
+        try:
+            gold, _ = searchbatch(self, ctx, Q, k)
+        finally:
+            self.set_param("plain", 0)
+        from .perf import macrorecall
+        chosen = candidates[-1]
+        for c in candidates:
+            self.set_param("overfetch", c)
+            ids, _ = searchbatch(self, ctx, Q, k)
+            if macrorecall(gold, ids) >= target_recall:
+                chosen = c
+                break
+        self.set_param("overfetch", chosen)
+        return chosen
+
     def _queries(self, Q) -> np.ndarray:
         Qdb = as_database(Q)
         rows = Qdb.rows()

@@ -119,3 +119,14 @@ def test_fp8_splits_and_allknn(ss, splits):
     fi, _ = O.searchbatch_f64("normcosine", X, X[rows], 9)
     gold = np.array([[i for i in fi[r] if i != j + 1][:8] for r, j in enumerate(rows)], dtype=np.uint32)
     assert O.macrorecall(gold, gi[rows]) >= 0.99
+
+
+@pytest.mark.parametrize("precision", ["fp8", "bf16"])
+def test_streaming_many_splits_merge_passes(ss, precision):
+    rng = np.random.default_rng(21)
+    X = mixture(rng, 20000, 384)
+    Q = X[rng.integers(0, 20000, size=40)] + rng.standard_normal((40, 384), dtype=np.float32) * 0.02
+    gi, gd = run(ss, "sql2", X, Q, 100, precision, overfetch=1.25, splits=120)
+    check_exact("sql2", X, Q, gi, gd, rows=4)
+    ri, _ = O.searchbatch("sql2", X, Q, 100)
+    assert O.macrorecall(ri, gi) >= 0.97

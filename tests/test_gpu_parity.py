@@ -111,6 +111,21 @@ def test_splits_do_not_change_results(ss, splits):
     assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
 
 
+@pytest.mark.parametrize("splits,k", [(64, 200), (148, 130), (40, 500)])
+def test_many_splits_need_merge_passes(ss, splits, k):
+    # splits x k candidates beyond one merge block go through reduction passes
+    rng = np.random.default_rng(splits + k)
+    X = rng.standard_normal((30000, 20), dtype=np.float32)
+    Q = rng.standard_normal((50, 20), dtype=np.float32)
+    for name in ("sql2", "normcosine"):
+        gi, gd, _, _ = gpu_search(ss, dist_of(ss, name), X, Q, k, splits=splits)
+        ri, rd = O.searchbatch(name, X, Q, k)
+        assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+    gi, gd, _, _ = gpu_search(ss, ss.Dist.SqL2(), X, Q, k, splits=splits, exact_scan=1)
+    ri, rd = O.searchbatch("sql2", X, Q, k)
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
 @pytest.mark.parametrize("k", [1, 4, 300, 305])
 def test_parallel_exhaustive_k_cases(ss, k):
     # test/testparallelexhaustive.jl:21-37: k in {1, 4, n, n+5} on n=300, dim=6
