@@ -662,6 +662,79 @@ def c4_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def c5_arm(args):
+    """C5: the learned shortlist on the C4 database under SqL2 (768 -> 256 ->
+    64 network, 200k-object sample, 5M triplets, 20 epochs, shortlist 512,
+    exact FP32 rerank to k = 10) beside the plain FP32 method and the same
+    pipeline with a 64-d random projection instead of the trained network."""
+    cx = Ctx()
+    torch, N, L = cx.torch, cx.N, cx.L
+    from oracle import oracle as O
+    X, Q, _, _ = make_c4(args.n if args.n is not None else 2_000_000, batches=200)
+    n, d = X.shape
+    m, k = min(10_000, Q.shape[0]), 10
+    Q = np.ascontiguousarray(Q[:m])
+    h = C.c_void_p()
+    N.check(L.ssg_create(N.METRIC_SQL2, N.ELEM_F32, d, n, X.ctypes.data_as(C.c_void_p), d, PREC["fp32"],
+                         C.byref(h)))
+    N.check(L.ssg_set_stream(h, C.c_void_p(torch.cuda.current_stream().cuda_stream)), h)
+    Qd = torch.from_numpy(Q).cuda()
+    ids_d = torch.empty((m, k), dtype=torch.int32, device="cuda")
+    dd_d = torch.empty((m, k), dtype=torch.float32, device="cuda")
+
+    def get(key):
+        v = C.c_double()
+        N.check(L.ssg_get_param(h, key.encode(), C.byref(v)), h)
+        return v.value
+
+    def timed(steps, warmup):
+        for _ in range(warmup):
+            N.check(L.ssg_search_device(h, C.c_void_p(Qd.data_ptr()), m, k, C.c_void_p(ids_d.data_ptr()),
+                                        C.c_void_p(dd_d.data_ptr()), 0), h)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            N.check(L.ssg_search_device(h, C.c_void_p(Qd.data_ptr()), m, k, C.c_void_p(ids_d.data_ptr()),
+                                        C.c_void_p(dd_d.data_ptr()), 0), h)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        return m / dt, dt * 1e3, ids_d.cpu().numpy().view(np.uint32).copy(), int(get("learned_used"))
+
+    steps, warmup = max(1, args.steps), max(1, args.warmup)
+    qps_plain, ms_plain, gold, _ = timed(1, 1)
+    # random projection: the pipeline without a trained network
+    N.check(L.ssg_set_param(h, b"learned_target", 0.0), h)
+    N.check(L.ssg_train_mlp(h, 200_000, 0, 0, 0, 64, 1024, 1e-3, 15), h)
+    rp_est = get("learned_recall")
+    qps_rp, ms_rp, got_rp, _ = timed(steps, warmup)
+    # the trained network
+    N.check(L.ssg_set_param(h, b"learned_target", 0.99), h)
+    N.check(L.ssg_train_mlp(h, 200_000, args.triplets, args.epochs, 256, 64, 1024, 1e-3, 15), h)
+    stats = {key: get(key) for key in ("learned_recall", "train_loss", "train_seconds", "train_steps")}
+    with ClockSampler(cx.local) as clk:
+        qps_l, ms_l, got_l, used = timed(steps, warmup)
+    # FP64 oracle on a sample of the queries
+    ns = 16
+    fi, _ = O.searchbatch_f64("sql2", X, Q[:ns], k, nthreads=os.cpu_count() or 1)
+    L.ssg_destroy(h)
+    line = {"metric": "queries/s (c5 learned shortlist)", "value": qps_l, "unit": "queries/s",
+            "n_gpus": cx.world, "steps": steps, "warmup": warmup, "ms_per_step": ms_l, "higher_is_better": True,
+            "vs_baseline": None, "dtype": "fp32 rerank, bf16-operand network",
+            "data": "synthetic, seeded 4096-cluster mixture, log-normal norms",
+            "config": {"workload": f"SqL2 searchbatch m={m}, k={k}, n={n:,}, d={d}; MLP {d}->256->64, "
+                                   f"200k sample, {args.triplets:,} triplets, {args.epochs} epochs, shortlist 512",
+                       "learned_used": used},
+            "recall@10_vs_plain": O.macrorecall(gold, got_l),
+            "recall@10_vs_fp64_sample": {"learned": O.macrorecall(fi, got_l[:ns]),
+                                         "plain": O.macrorecall(fi, gold[:ns]), "queries": ns},
+            "estimated_recall": stats["learned_recall"], "training": stats,
+            "random_projection": {"value": qps_rp, "recall@10_vs_plain": O.macrorecall(gold, got_rp),
+                                  "estimated_recall": rp_est},
+            "plain_fp32": {"value": qps_plain, "ms_per_step": ms_plain},
+            "speedup_vs_plain": qps_l / qps_plain, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_DB
     ap = argparse.ArgumentParser()
@@ -670,11 +743,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--mode", default=HEADLINE_MODE, choices=["fp32", "bf16", "fp8"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 = the headline allknn workload; c1 / c3 = the suite's other searchbatch workloads")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--cpu-queries", type=int, default=64, help="c1/c3: queries timed on the CPU")
     ap.add_argument("--batches", type=int, default=200, help="c4: batches in the request stream")
+    ap.add_argument("--triplets", type=int, default=5_000_000, help="c5: training triplets")
+    ap.add_argument("--epochs", type=int, default=20, help="c5: training epochs")
     ap.add_argument("--n", type=int, default=None,
                     help="database size (profiling captures use a smaller case of the same workload)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
@@ -688,6 +763,8 @@ def main():
         reference_arm(args)
     elif args.workload == "c4":
         c4_arm(args)
+    elif args.workload == "c5":
+        c5_arm(args)
     elif args.workload != "c2":
         workload_arm(args)
     else:

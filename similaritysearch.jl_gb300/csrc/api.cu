@@ -78,6 +78,11 @@ struct ssg_index {
     // the completeness check and the fallback's buffers
     DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand;
     DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
+    // learned shortlist (trained model, whether searches use it, recall target)
+    ssg::LearnedModel *learned = nullptr;
+    int learned_param = 1;
+    double learned_target = 0.99;
+    int last_learned = 0;
     float max_x_sq = 0.0f;
     int margin_param = 0;
     int exact_scan_param = 0;
@@ -793,6 +798,83 @@ struct Guard {
     }
 };
 
+double learned_recall(const ssg_index *idx) {
+    bool found = false;
+    return ssg::learned_get(idx->learned, "learned_recall", &found);
+}
+
+ssg::IndexView view_of(ssg_index *idx) {
+    ssg::IndexView v;
+    v.db = static_cast<const float *>(idx->db.p);
+    v.db_norm = static_cast<const float *>(idx->db_norm.p);
+    v.n = idx->n;
+    v.dim = idx->dim;
+    v.metric = idx->metric;
+    v.stream = idx->stream;
+    v.launches = &idx->last_launches;
+    return v;
+}
+
+// Whether a search goes through the learned shortlist: a model exists, the
+// caller has not switched it off, and its estimated recall meets the target
+// (otherwise the plain exhaustive method answers: the fallback).
+bool use_learned(const ssg_index *idx) {
+    return idx->learned && idx->learned_param && !idx->plain_param && idx->metric != SSG_METRIC_HAMMING &&
+           learned_recall(idx) >= idx->learned_target;
+}
+
+// Recall@10 of the learned pipeline against the plain method on 256 random
+// objects of the database used as queries; stored with the model.
+int estimate_learned_recall(ssg_index *idx, uint64_t seed) {
+    const int64_t mq = std::min<int64_t>(256, idx->n);
+    const int k = int(std::min<int64_t>(10, idx->n));
+    std::vector<int64_t> rows(static_cast<size_t>(mq));
+    uint64_t x = seed * 6364136223846793005ull + 1442695040888963407ull;
+    for (auto &r : rows) {
+        x = x * 6364136223846793005ull + 1442695040888963407ull;
+        r = int64_t((x >> 11) % uint64_t(idx->n));
+    }
+    DevBuf qrows, dlist, gold, got;
+    SSG_CK(dlist.ensure(size_t(mq) * 8), "allocating recall queries");
+    SSG_CK(qrows.ensure(size_t(mq) * idx->dim * 4), "allocating recall queries");
+    SSG_CK(gold.ensure(size_t(mq) * k * 8), "allocating recall results");
+    SSG_CK(got.ensure(size_t(mq) * k * 8), "allocating recall results");
+    SSG_CK(cudaMemcpyAsync(dlist.p, rows.data(), size_t(mq) * 8, cudaMemcpyHostToDevice, idx->stream), "copying");
+    SSG_CK(ssg::launch_gather_rows(idx->db.p, static_cast<const int64_t *>(dlist.p), mq, size_t(idx->dim) * 4,
+                                   qrows.p, idx->stream, &idx->last_launches),
+           "gathering recall queries");
+    const float *qn = nullptr;
+    if (idx->metric == SSG_METRIC_COSINE) {
+        SSG_CK(idx->qnorm.ensure(size_t(mq) * 4), "allocating query norms");
+        SSG_CK(ssg::launch_row_norms(static_cast<const float *>(qrows.p), mq, idx->dim,
+                                     static_cast<float *>(idx->qnorm.p), idx->stream, &idx->last_launches),
+               "computing query norms");
+        qn = static_cast<const float *>(idx->qnorm.p);
+    }
+    uint32_t *gi = static_cast<uint32_t *>(gold.p);
+    float *gd = reinterpret_cast<float *>(gi + size_t(mq) * k);
+    const int saved = idx->plain_param;
+    idx->plain_param = 1;
+    int rc = run_knn(idx, qrows.p, qn, mq, k, 0, gi, gd);
+    idx->plain_param = saved;
+    if (rc) return rc;
+    uint32_t *li = static_cast<uint32_t *>(got.p);
+    float *ld = reinterpret_cast<float *>(li + size_t(mq) * k);
+    std::string err;
+    rc = ssg::learned_search(idx->learned, view_of(idx), static_cast<const float *>(qrows.p), qn, mq, k, li, ld, err);
+    if (rc) return fail(idx, rc, "learned search: %s", err.c_str());
+    std::vector<uint32_t> hg(size_t(mq) * k), hl(size_t(mq) * k);
+    SSG_CK(cudaMemcpy(hg.data(), gi, hg.size() * 4, cudaMemcpyDeviceToHost), "reading recall results");
+    SSG_CK(cudaMemcpy(hl.data(), li, hl.size() * 4, cudaMemcpyDeviceToHost), "reading recall results");
+    double hit = 0.0;
+    for (int64_t j = 0; j < mq; ++j)
+        for (int a = 0; a < k; ++a)
+            for (int b = 0; b < k; ++b)
+                if (hg[size_t(j) * k + a] == hl[size_t(j) * k + b]) { hit += 1.0; break; }
+    ssg::learned_set_recall(idx->learned, hit / double(mq * k));
+    return SSG_OK;
+}
+
 int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t k, uint32_t *ids,
                   float *dists, int32_t flags, bool device) {
     if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
@@ -822,8 +904,17 @@ int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t
         d_ids = static_cast<uint32_t *>(idx->outbuf.p);
         d_dists = reinterpret_cast<float *>(static_cast<char *>(idx->outbuf.p) + size_t(m) * k * 4);
     }
-    rc = run_knn(idx, dq, dqn, m, k, 0, d_ids, d_dists);
-    if (rc) return rc;
+    idx->last_learned = 0;
+    if (use_learned(idx)) {
+        std::string err;
+        rc = ssg::learned_search(idx->learned, view_of(idx), static_cast<const float *>(dq), dqn, m, k, d_ids, d_dists,
+                                 err);
+        if (rc) return fail(idx, rc, "learned search: %s", err.c_str());
+        idx->last_learned = 1;
+    } else {
+        rc = run_knn(idx, dq, dqn, m, k, 0, d_ids, d_dists);
+        if (rc) return rc;
+    }
     if (!device) {
         SSG_CK(cudaMemcpyAsync(ids, d_ids, size_t(m) * k * 4, cudaMemcpyDeviceToHost, idx->stream), "copying ids");
         SSG_CK(cudaMemcpyAsync(dists, d_dists, size_t(m) * k * 4, cudaMemcpyDeviceToHost, idx->stream),
@@ -921,7 +1012,13 @@ int ssg_append(ssg_index *idx, const void *host_rows, int64_t count) {
     if (count == 0) return SSG_OK;
     if (!host_rows) return fail(idx, SSG_EINVAL, "rows pointer is NULL");
     if (idx->n + count >= (int64_t(1) << 32) - 1) return fail(idx, SSG_EINVAL, "too many objects");
-    return add_rows(idx, host_rows, count, idx->dim, false);
+    int rc = add_rows(idx, host_rows, count, idx->dim, false);
+    if (rc || !idx->learned) return rc;
+    // the learned shortlist must cover the new objects: embed the database again
+    std::string err;
+    rc = ssg::learned_index_db(idx->learned, view_of(idx), err);
+    if (rc) return fail(idx, rc, "re-indexing the learned shortlist: %s", err.c_str());
+    return SSG_OK;
 }
 
 int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len, uint32_t *ids, float *dists) {
@@ -967,6 +1064,17 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->exact_scan_param = value != 0.0;
     } else if (k == "plain") {
         idx->plain_param = value != 0.0;
+    } else if (k == "learned") {
+        idx->learned_param = value != 0.0;
+    } else if (k == "learned_target") {
+        if (!(value >= 0.0 && value <= 1.0)) return fail(idx, SSG_EINVAL, "learned_target must be in [0, 1]");
+        idx->learned_target = value;
+    } else if (k == "shortlist") {
+        if (!(value >= 1 && value <= 4096)) return fail(idx, SSG_EINVAL, "shortlist must be in [1, 4096]");
+        if (!ssg::learned_set(idx->learned, "shortlist", value))
+            return fail(idx, SSG_EINVAL, "no learned model on this index");
+        // the recall estimate belongs to the shortlist length: measure it again
+        return estimate_learned_recall(idx, 12345);
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -993,13 +1101,21 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "margin") *value = idx->margin_param;
     else if (k == "exact_scan") *value = idx->exact_scan_param;
     else if (k == "plain") *value = idx->plain_param;
+    else if (k == "learned") *value = idx->learned_param;
+    else if (k == "learned_target") *value = idx->learned_target;
+    else if (k == "learned_used") *value = idx->last_learned;
     else if (k == "fallbacks") *value = idx->last_fallbacks;
     else if (k == "max_x_sq") *value = idx->max_x_sq;
     else if (k == "device_bytes")
         *value = double(idx->db.bytes + idx->db_norm.bytes + idx->qbuf.bytes + idx->qnorm.bytes + idx->cand.bytes +
                         idx->gheap.bytes + idx->outbuf.bytes + idx->stage.bytes + idx->tc_db.bytes +
                         idx->tc_norm.bytes + idx->tc_q.bytes);
-    else return fail(idx, SSG_EINVAL, "unknown parameter '%s'", key);
+    else {
+        bool found = false;
+        const double v = ssg::learned_get(idx->learned, key, &found);
+        if (!found) return fail(idx, SSG_EINVAL, "unknown parameter '%s'", key);
+        *value = v;
+    }
     return SSG_OK;
 }
 
@@ -1023,6 +1139,69 @@ int ssg_last_error(ssg_index *idx, char *buf, int64_t len) {
     return full;
 }
 
+int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t epochs, int32_t hidden,
+                  int32_t out_dim, int32_t batch, double lr, uint64_t seed) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (idx->metric == SSG_METRIC_HAMMING)
+        return fail(idx, SSG_EUNSUPPORTED, "the learned shortlist is for float metrics");
+    if (idx->n < 32) return fail(idx, SSG_EINVAL, "the index needs at least 32 objects to train on");
+    if (sample_n < 12 || triplets < 0 || epochs < 0 || hidden < 0 || hidden > 8192 || out_dim < 1 ||
+        out_dim > 1024 || batch < 1 || batch > 65536 || !(lr > 0.0))
+        return fail(idx, SSG_EINVAL, "invalid training arguments");
+    ssg::TrainArgs t{};
+    t.sample = sample_n;
+    t.triplets = triplets;
+    t.epochs = epochs;
+    t.hidden = hidden;
+    t.out_dim = out_dim;
+    t.batch = batch;
+    t.lr = float(lr);
+    t.margin = 1.0f;
+    t.seed = seed;
+    t.shortlist = 512;
+    ssg::LearnedModel *m = nullptr;
+    std::string err;
+    int rc = ssg::learned_train(view_of(idx), t, &m, err);
+    if (rc) return fail(idx, rc, "training failed: %s", err.c_str());
+    ssg::learned_free(idx->learned);
+    idx->learned = m;
+    return estimate_learned_recall(idx, seed);
+}
+
+int ssg_save_model(ssg_index *idx, const char *path) {
+    if (!idx || !path) return fail(idx, SSG_EINVAL, "NULL argument");
+    Guard g(idx, false);
+    if (!idx->learned) return fail(idx, SSG_EINVAL, "no learned model on this index");
+    std::string err;
+    int rc = ssg::learned_save(idx->learned, path, err);
+    return rc ? fail(idx, rc, "%s", err.c_str()) : SSG_OK;
+}
+
+int ssg_load_model(ssg_index *idx, const char *path) {
+    if (!idx || !path) return fail(idx, SSG_EINVAL, "NULL argument");
+    Guard g(idx);
+    ssg::LearnedModel *m = nullptr;
+    std::string err;
+    int rc = ssg::learned_load(view_of(idx), path, &m, err);
+    if (rc) return fail(idx, rc, "%s", err.c_str());
+    ssg::learned_free(idx->learned);
+    idx->learned = m;
+    return estimate_learned_recall(idx, 12345);
+}
+
+int ssg_mlp_grad_check(int64_t d, int64_t hidden, int64_t out_dim, const float *W1, const float *b1, const float *W2,
+                       const float *b2, const float *X, int32_t batch, float margin, float *loss, float *gW1,
+                       float *gb1, float *gW2, float *gb2) {
+    if (d <= 0 || hidden <= 0 || out_dim <= 0 || batch <= 0 || !W1 || !b1 || !W2 || !b2 || !X || !loss || !gW1 ||
+        !gb1 || !gW2 || !gb2)
+        return fail(nullptr, SSG_EINVAL, "invalid gradient-check arguments");
+    std::string err;
+    int rc = ssg::learned_grad_check(d, hidden, out_dim, W1, b1, W2, b2, X, batch, margin, loss, gW1, gb1, gW2, gb2,
+                                     err);
+    return rc ? fail(nullptr, rc, "%s", err.c_str()) : SSG_OK;
+}
+
 void ssg_destroy(ssg_index *idx) {
     if (!idx) return;
     cudaSetDevice(idx->device);
@@ -1040,6 +1219,8 @@ void ssg_destroy(ssg_index *idx) {
     idx->tc_norm.release();
     idx->tc_q.release();
     idx->status.release();
+    ssg::learned_free(idx->learned);
+    idx->learned = nullptr;
     for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale,
                       &idx->red[0], &idx->red[1]})
         b->release();

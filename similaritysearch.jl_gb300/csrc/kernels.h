@@ -1,6 +1,7 @@
 // kernels.h -- host-side launchers of the device kernels (internal to libssgpu).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace ssg {
@@ -147,6 +148,51 @@ cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, 
                                    int k, uint32_t *ids, float *dists, cudaStream_t st, int *launches);
 
 int device_sm_count();
+
+// ---- learned shortlist (mlp.cu, learned.cu) ----
+// C[M x N] = op(A) op(B) (+bias) (ReLU): op(A) = A (M x K) or A^T (A is K x M,
+// ta); op(B) = B^T (B is N x K) or B (B is K x N, tb); bf16 rounds operands.
+cudaError_t mlp_gemm(const float *A, const float *B, const float *bias, float *C, int M, int N, int K, int ta, int tb,
+                     int relu, int bf16, int accumulate, cudaStream_t st, int *launches);
+cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
+                        cudaStream_t st, int *launches);
+cudaError_t mlp_relu_backward(float *dH, const float *H, int64_t count, cudaStream_t st, int *launches);
+cudaError_t mlp_colsum(const float *G, int rows, int N, float *out, cudaStream_t st, int *launches);
+cudaError_t mlp_adam(float *W, const float *G, float *M, float *V, int64_t count, float lr, int step,
+                     cudaStream_t st, int *launches);
+
+// What the learned code needs of an index.
+struct IndexView {
+    const float *db;
+    const float *db_norm;
+    int64_t n, dim;
+    int metric;
+    cudaStream_t stream;
+    int *launches;
+};
+struct TrainArgs {
+    int64_t sample, triplets;
+    int epochs;
+    int64_t hidden, out_dim;
+    int batch;
+    float lr, margin;
+    uint64_t seed;
+    int shortlist;
+};
+struct LearnedModel;
+void learned_free(LearnedModel *m);
+double learned_get(const LearnedModel *m, const char *key, bool *found);
+bool learned_set(LearnedModel *m, const char *key, double v);
+int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, std::string &err);
+int learned_index_db(LearnedModel *m, const IndexView &v, std::string &err);
+int learned_search(LearnedModel *m, const IndexView &v, const float *dq, const float *dqn, int64_t mq, int k,
+                   uint32_t *d_ids, float *d_dists, std::string &err);
+int learned_save(const LearnedModel *m, const char *path, std::string &err);
+int learned_load(const IndexView &v, const char *path, LearnedModel **out, std::string &err);
+void learned_set_recall(LearnedModel *m, double r);
+int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const float *b1, const float *W2,
+                       const float *b2, const float *X, int B, float margin, float *loss, float *gW1, float *gb1,
+                       float *gW2, float *gb2, std::string &err);
 
 // Records `msg` as the calling thread's last error (what ssg_last_error(NULL,
 // ...) returns) and returns `code`.

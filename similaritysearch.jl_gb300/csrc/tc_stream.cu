@@ -241,8 +241,13 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
         uint64_t *heap = heap_base + (e * 32 + lane);
         uint64_t *cbuf = buf_base + (e * 32 + lane);
         Heap{heap, a.kk, hs}.init();
+        // padding rows of a partial query tile filter everything out (a
+        // -inf threshold), and warps holding only padding rows skip the
+        // epilogue: they just hand the accumulator back
+        const bool qvalid = query < a.m;
+        const bool warp_live = __any_sync(0xffffffffu, qvalid);
         uint64_t top = KEY_EMPTY;
-        float topd = INFINITY;
+        float topd = qvalid ? INFINITY : -INFINITY;
         int nbuf = 0;
         for (int t = 0; t < T_tiles; ++t) {
             const int b = t & 1;
@@ -251,6 +256,12 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
+            if (!warp_live) {
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+                continue;
+            }
             const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
             uint32_t r[CHUNKS][32];
             __syncwarp();
@@ -292,7 +303,7 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                         if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
                             top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
                             nbuf = 0;
-                            topd = (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                            topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
                         }
                     }
                 }

@@ -153,6 +153,34 @@ class GPUExhaustiveSearch:
         self.set_param("overfetch", chosen)
         return chosen
 
+    def train_mlp(self, sample: int = 50_000, triplets: int = 200_000, epochs: int = 4, hidden: int = 256,
+                  out_dim: int = 64, batch: int = 1024, lr: float = 1e-3, seed: int = 1,
+                  target_recall: float | None = None) -> dict:
+        """Trains the learned shortlist (``ssg_train_mlp``): a d -> hidden ->
+        out_dim network under a triplet loss whose positives are exact
+        neighbours found by this index, then indexes the embedded database.
+        ``hidden=0`` builds the untrained random-projection baseline instead.
+        Searches take the learned path while the estimated recall@10 against
+        the plain method reaches ``target_recall`` (default 0.99), the plain
+        method otherwise.  Returns the training statistics."""
+        if target_recall is not None:
+            self.set_param("learned_target", target_recall)
+        N.check(N.lib().ssg_train_mlp(self._h, int(sample), int(triplets), int(epochs), int(hidden), int(out_dim),
+                                      int(batch), float(lr), int(seed)), self._h)
+        return self.learned_stats()
+
+    def learned_stats(self) -> dict:
+        keys = ("learned_ready", "learned_recall", "learned_target", "train_loss", "train_seconds", "train_steps",
+                "shortlist")
+        return {k: self.get_param(k) for k in keys}
+
+    def save_model(self, path: str):
+        N.check(N.lib().ssg_save_model(self._h, str(path).encode()), self._h)
+
+    def load_model(self, path: str) -> dict:
+        N.check(N.lib().ssg_load_model(self._h, str(path).encode()), self._h)
+        return self.learned_stats()
+
     def _queries(self, Q) -> np.ndarray:
         Qdb = as_database(Q)
         rows = Qdb.rows()
