@@ -268,15 +268,12 @@ class Ctx:
             dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
         ss = load_package()
         ss.build()
+        self.ss = ss
         self.N = ss._native
         self.L = self.N.lib()
 
     def max_over_ranks(self, v):
-        if self.world == 1:
-            return v
-        t = self.torch.tensor([v], device="cuda")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
-        return float(t.item())
+        return self.ss.shard.max_over_ranks(v, device="cuda")
 
     def barrier(self):
         if self.world > 1:

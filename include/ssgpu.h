@@ -165,7 +165,8 @@ int ssg_version(void);
  * method, measured on 256 database objects when the model is trained or
  * loaded) is at least "learned_target" (default 0.99) and "learned" is 1;
  * otherwise the index's own method answers.  "learned_used" tells whether the
- * last search took the learned path.  Float metrics only.
+ * last search took the learned path.  Float metrics only; 1 <= out_dim <= 256,
+ * hidden <= 8192.
  * Readable keys: "learned_recall", "learned_ready", "train_loss",
  * "train_seconds", "train_steps", "shortlist". */
 int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t epochs,

@@ -4,7 +4,7 @@ Host-side mirror of the reference's ``searchbatch`` / ``allknn`` path over a
 GPU index (``GPUExhaustiveSearch``) whose work is done by libssgpu.so, the
 sm_103a CUDA library with the C ABI of ``include/ssgpu.h``.
 """
-from . import _native
+from . import _native, shard
 from .db import AbstractDatabase, MatrixDatabase, VectorDatabase
 from .dist import Dist, PreMetric, evaluate
 from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,

@@ -76,7 +76,11 @@ struct ssg_index {
     DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
     // plain FP32 GEMM-form path: |x|^2 per row and its maximum, query flags of
     // the completeness check and the fallback's buffers
-    DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand;
+    DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand, fb_qn;
+    // BF16 threshold-filter path (candidate counts beyond the on-chip heaps):
+    // tiles of every smp_r-th database row, filtered lists, counts, bounds
+    DevBuf tc_smp, tc_smp_norm, f_out, f_cnt, f_thr;
+    int64_t smp_r = 0, smp_n = -1, smp_rows = 0;
     DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
     // learned shortlist (trained model, whether searches use it, recall target)
     ssg::LearnedModel *learned = nullptr;
@@ -330,6 +334,23 @@ int create_common(int metric, int elem, int64_t dim, int64_t n, const void *src,
 // Picks the number of database splits per query tile: enough blocks to fill
 // the GPU several times over, while every split stays long enough to amortise
 // its heap and the merge stays within one block's shared memory.
+// Database splits per query tile for a kernel with `cap` resident CTAs on the
+// device: qctas * s CTAs run in ceil(qctas * s / cap) waves, each CTA scanning
+// 1/s of the database, so the scan takes ~ waves(s) / s.  Minimise that, with
+// a 1% charge per extra split for the wider merge, over s <= max_s.
+int64_t wave_splits(int64_t qctas, int64_t cap, int64_t max_s) {
+    qctas = std::max<int64_t>(1, qctas);
+    const int64_t hi = std::max<int64_t>(1, std::min<int64_t>(max_s, 4 * ((cap + qctas - 1) / qctas)));
+    int64_t best = 1;
+    double best_cost = 1e300;
+    for (int64_t sp = 1; sp <= hi; ++sp) {
+        const double waves = double((qctas * sp + cap - 1) / cap);
+        const double cost = waves / double(sp) * (1.0 + 0.01 * double(sp - 1));
+        if (cost < best_cost * (1.0 - 1e-9)) { best_cost = cost; best = sp; }
+    }
+    return best;
+}
+
 int choose_splits(ssg_index *idx, int64_t m, int kk, int qpb) {
     if (idx->splits_param > 0) return idx->splits_param;
     const int64_t qtiles = (m + qpb - 1) / qpb;
@@ -467,13 +488,18 @@ int gemm_margin(const ssg_index *idx, int take) {
 // metrics get exact keys directly; SqL2 / L2 re-score kk = k + margin
 // candidates exactly, and queries whose margin is not provably enough are
 // recomputed with the exact direct scan.
+int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, const int *flags, int nflag,
+                 uint32_t *d_ids, float *d_dists);
+
 int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k, int exclude_self,
              uint32_t *d_ids, float *d_dists, int kk) {
     const int take = k + (exclude_self ? 1 : 0);
     const bool sq = is_sq_metric(idx->metric);
     const int64_t qtiles = (m + 127) / 128;
-    int64_t splits = idx->splits_param > 0 ? idx->splits_param
-                                           : (ssg::device_sm_count() + qtiles - 1) / qtiles;
+    int64_t splits = idx->splits_param > 0
+                         ? idx->splits_param
+                         : wave_splits(qtiles, int64_t(ssg::gemm_ctas_per_sm(kk)) * ssg::device_sm_count(),
+                                       std::max<int64_t>(1, idx->n / 512));
     splits = std::min<int64_t>(splits, std::max<int64_t>(1, idx->n / 512));
     splits = std::max<int64_t>(1, splits);
     const int64_t split_len = (idx->n + splits - 1) / splits;
@@ -543,6 +569,13 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
     SSG_CK(cudaMemcpyAsync(&nflag, flag_count, sizeof(int), cudaMemcpyDeviceToHost, idx->stream), "reading flags");
     SSG_CK(cudaStreamSynchronize(idx->stream), "running the FP32 scan");
     idx->last_fallbacks = nflag;
+    return run_fallback(idx, dq, m, k, exclude_self, flags, nflag, d_ids, d_dists);
+}
+
+// Recomputes the flagged queries (flags[j] != 0, nflag of them) with the exact
+// direct scan and scatters their rows into the results.
+int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, const int *flags, int nflag,
+                 uint32_t *d_ids, float *d_dists) {
     if (nflag == 0) return SSG_OK;
     std::vector<int> hflags(static_cast<size_t>(m), 0);
     SSG_CK(cudaMemcpy(hflags.data(), flags, size_t(m) * 4, cudaMemcpyDeviceToHost), "reading flags");
@@ -562,7 +595,15 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
            "gathering fallback queries");
     uint32_t *fi = static_cast<uint32_t *>(idx->fb_out.p);
     float *fd = reinterpret_cast<float *>(fi + size_t(cnt) * k);
-    SSG_RC(run_exact_scan(idx, idx->fb_q.p, nullptr, cnt, k, exclude_self, dlist, fi, fd, idx->fb_cand));
+    const float *fqn = nullptr;
+    if (idx->metric == SSG_METRIC_COSINE) {
+        SSG_CK(idx->fb_qn.ensure(size_t(cnt) * 4), "allocating fallback query norms");
+        SSG_CK(ssg::launch_row_norms(static_cast<const float *>(idx->fb_q.p), cnt, idx->dim,
+                                     static_cast<float *>(idx->fb_qn.p), idx->stream, &idx->last_launches),
+               "computing fallback query norms");
+        fqn = static_cast<const float *>(idx->fb_qn.p);
+    }
+    SSG_RC(run_exact_scan(idx, idx->fb_q.p, fqn, cnt, k, exclude_self, dlist, fi, fd, idx->fb_cand));
     SSG_CK(ssg::launch_scatter_results(fi, fd, dlist, cnt, k, d_ids, d_dists, idx->stream, &idx->last_launches),
            "scattering fallback results");
     SSG_CK(cudaStreamSynchronize(idx->stream), "running the fallback scan");
@@ -596,6 +637,9 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
 // The BF16 pipeline: operand tiles of the queries (or the database itself for
 // allknn), the tcgen05 scan keeping kk = overfetch * k approximate candidates
 // per query and split, then the exact FP32 rerank + (distance, id) merge.
+int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                      uint32_t *d_ids, float *d_dists, bool queries_are_db, int kk);
+
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db) {
     const int take = k + (exclude_self ? 1 : 0);
@@ -603,17 +647,19 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     kk64 = std::max<int64_t>(kk64, take);
     kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
     const int kp = ssg::tc_padded_k(idx->dim);
-    // the over-fetch is capped by what the kernel's on-chip heaps hold
     int kk = int(kk64);
     int qt = 0, stages = 0;
-    while (kk > take && !ssg::tc_choose(kp, kk, &qt, &stages)) --kk;
+    idx->last_fallbacks = 0;
+    // more candidates than the kernel's on-chip heaps hold: threshold filter
+    if (!ssg::tc_choose(kp, kk, &qt, &stages))
+        return run_knn_tc_filter(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db, kk);
     if (!ssg::tc_choose(kp, kk, &qt, &stages))
         return fail(idx, SSG_EUNSUPPORTED, "k = %d does not fit the BF16 kernel's on-chip top-k", take);
     const int64_t qrows = int64_t(qt) * 128;
     const int64_t qctas = (m + qrows - 1) / qrows;
     const int64_t n_tiles = ssg::tc_tiles(idx->n);
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
-                                           : (ssg::device_sm_count() + qctas - 1) / qctas;
+                                           : wave_splits(qctas, ssg::device_sm_count(), n_tiles);
     splits = std::min<int64_t>(splits, n_tiles);
     splits = std::max<int64_t>(1, splits);
     // chunk the queries (a multiple of the CTA's query rows) to bound scratch
@@ -677,6 +723,144 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     return SSG_OK;
 }
 
+// BF16 tiles of every r-th database row (the sample that sets the filter
+// bounds), rebuilt when r or the database changes.
+int ensure_sample_tiles(ssg_index *idx, int64_t r) {
+    if (idx->smp_r == r && idx->smp_n == idx->n) return SSG_OK;
+    const int64_t ns = (idx->n + r - 1) / r;
+    std::vector<int64_t> rows(static_cast<size_t>(ns));
+    for (int64_t i = 0; i < ns; ++i) rows[size_t(i)] = i * r;
+    DevBuf list, xs;
+    SSG_CK(list.ensure(size_t(ns) * 8), "allocating the sample list");
+    SSG_CK(xs.ensure(size_t(ns) * idx->dim * 4), "allocating sample rows");
+    SSG_CK(cudaMemcpyAsync(list.p, rows.data(), size_t(ns) * 8, cudaMemcpyHostToDevice, idx->stream),
+           "copying the sample list");
+    SSG_CK(ssg::launch_gather_rows(idx->db.p, static_cast<const int64_t *>(list.p), ns, size_t(idx->dim) * 4, xs.p,
+                                   idx->stream, &idx->last_launches),
+           "gathering sample rows");
+    const int64_t tiles = (ssg::tc_tiles(ns) + 1) / 2 * 2;
+    SSG_CK(idx->tc_smp.ensure(size_t(tiles) * ssg::tc_tile_bytes(idx->dim)), "allocating sample tiles");
+    SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(xs.p), ns, idx->dim, tiles,
+                                  static_cast<uint8_t *>(idx->tc_smp.p), idx->stream, &idx->last_launches),
+           "building sample tiles");
+    SSG_CK(idx->tc_smp_norm.ensure(size_t(tiles) * 128 * 4), "allocating sample norms");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, static_cast<const float *>(xs.p), ns, idx->dim, tiles * 128,
+                                static_cast<float *>(idx->tc_smp_norm.p), idx->stream, &idx->last_launches),
+           "computing sample norms");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building sample tiles");
+    idx->smp_r = r;
+    idx->smp_n = idx->n;
+    idx->smp_rows = ns;
+    return SSG_OK;
+}
+
+// The BF16 pipeline for kk beyond the on-chip heaps (e.g. long shortlists).
+// A scan of every r-th database row keeps kSampleK candidates per query,
+// whose distance bounds a set of about 3 * kk candidates of the full
+// database; the full scan appends every candidate within the bound to the
+// query's list (fcap keys), the kk best are sorted out and re-ranked exactly.
+// Queries whose list came out shorter than kk or overflowed are recomputed
+// with the exact direct scan.  Databases of up to 8192 rows skip the sample:
+// every row is a candidate.
+int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                      uint32_t *d_ids, float *d_dists, bool queries_are_db, int kk) {
+    constexpr int kSampleK = 16;
+    const int64_t n = idx->n;
+    const bool all = n <= 8192;
+    const int fcap = all ? int(n) : 4096;
+    if (kk > fcap) return fail(idx, SSG_EUNSUPPORTED, "%d candidates exceed the filter's list capacity", kk);
+    const int64_t r = std::max<int64_t>(1, int64_t(3) * kk / (2 * kSampleK));
+    if (!all) {
+        SSG_RC(ensure_sample_tiles(idx, r));
+        if (idx->smp_rows < 4 * kSampleK)
+            return fail(idx, SSG_EUNSUPPORTED, "the database is too small for the filter's sample");
+    }
+    const int segs_s = ssg::tc_segments_per_split(1);
+    const size_t per_query = size_t(fcap) * 8 + size_t(std::max(kk, segs_s * kSampleK)) * 8 + 8;
+    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(512) << 20) / per_query) / 128 * 128);
+    chunk = std::min<int64_t>(chunk, (m + 127) / 128 * 128);
+    SSG_CK(idx->f_out.ensure(size_t(chunk) * fcap * 8), "allocating filter lists");
+    SSG_CK(idx->f_cnt.ensure(size_t(chunk) * 4), "allocating filter counts");
+    SSG_CK(idx->f_thr.ensure(size_t(chunk) * 4), "allocating filter bounds");
+    SSG_CK(idx->cand.ensure(size_t(chunk) * std::max(kk, segs_s * kSampleK) * 8), "allocating candidate scratch");
+    SSG_CK(idx->flags.ensure(size_t(m) * 4 + 16), "allocating query flags");
+    SSG_CK(cudaMemsetAsync(idx->flags.p, 0, size_t(m) * 4 + 16, idx->stream), "clearing query flags");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    int *flags = static_cast<int *>(idx->flags.p);
+    int *flag_count = flags + m;
+    int *status = static_cast<int *>(idx->status.p);
+    const size_t tb = ssg::tc_tile_bytes(idx->dim);
+    const uint8_t *qtiles = static_cast<const uint8_t *>(idx->tc_db.p);
+    if (!queries_are_db) {
+        const int64_t qt_alloc = (m + 127) / 128;
+        SSG_CK(idx->tc_q.ensure(size_t(qt_alloc) * tb), "allocating BF16 query tiles");
+        SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(dq), m, idx->dim, qt_alloc,
+                                      static_cast<uint8_t *>(idx->tc_q.p), idx->stream, &idx->last_launches),
+               "building BF16 query tiles");
+        qtiles = static_cast<const uint8_t *>(idx->tc_q.p);
+    }
+    const int64_t n_tiles = ssg::tc_tiles(n);
+    uint64_t *cand = static_cast<uint64_t *>(idx->cand.p);
+    float *thr = static_cast<float *>(idx->f_thr.p);
+    int *fcnt = static_cast<int *>(idx->f_cnt.p);
+    uint64_t *fout = static_cast<uint64_t *>(idx->f_out.p);
+    ScanTimer timer(idx);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        const int64_t qct = (mc + 127) / 128;
+        const uint8_t *qc_tiles = qtiles + size_t(c0 / 128) * tb;
+        if (all) {
+            // 0x7f7f7f7f is a finite bound above every distance
+            SSG_CK(cudaMemsetAsync(thr, 0x7f, size_t(mc) * 4, idx->stream), "setting filter bounds");
+        } else {
+            SSG_CK(ssg::launch_tc_scan(idx->metric, qc_tiles, static_cast<const uint8_t *>(idx->tc_smp.p),
+                                       static_cast<const float *>(idx->tc_smp_norm.p), idx->smp_rows, mc, idx->dim,
+                                       kSampleK, 1, cand, status, idx->stream, &idx->last_launches, nullptr),
+                   "launching the sample scan");
+            SSG_CK(ssg::launch_sample_bound(cand, mc, segs_s, kSampleK, thr, idx->stream, &idx->last_launches),
+                   "computing filter bounds");
+        }
+        SSG_CK(cudaMemsetAsync(fcnt, 0, size_t(mc) * 4, idx->stream), "clearing filter counts");
+        const int64_t splits = idx->splits_param > 0 ? std::min<int64_t>(idx->splits_param, n_tiles)
+                                                     : wave_splits(qct, ssg::device_sm_count(), n_tiles);
+        SSG_RC(timer.begin());
+        SSG_CK(ssg::launch_tc_filter(idx->metric, qc_tiles, static_cast<const uint8_t *>(idx->tc_db.p),
+                                     static_cast<const float *>(idx->tc_norm.p), n, mc, idx->dim, int(splits), thr,
+                                     fout, fcnt, fcap, status, idx->stream, &idx->last_launches),
+               "launching the BF16 filter scan");
+        SSG_RC(timer.end());
+        SSG_CK(ssg::launch_filter_select(fout, fcnt, mc, fcap, kk, cand, flags + c0, flag_count, idx->stream,
+                                         &idx->last_launches),
+               "selecting filtered candidates");
+        ssg::FinalizeArgs f{};
+        f.cand = cand;
+        f.segs = 1;
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim,
+                                           static_cast<const float *>(dq) + size_t(c0) * idx->dim,
+                                           dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches),
+               "launching the rerank kernel");
+        SSG_RC(timer.collect());
+    }
+    int hstatus = 0, nflag = 0;
+    SSG_CK(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaMemcpyAsync(&nflag, flag_count, sizeof(int), cudaMemcpyDeviceToHost, idx->stream), "reading flags");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the BF16 filter search");
+    if (hstatus != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the BF16 scan kernel gave up (code %d)", hstatus);
+    idx->last_fallbacks = nflag;
+    return run_fallback(idx, static_cast<const float *>(dq), m, k, exclude_self, flags, nflag, d_ids, d_dists);
+}
+
 // The K-streaming pipeline (FP8, or BF16 for wide vectors): operand tiles
 // of the queries (the database's own for allknn), the tcgen05 scan keeping
 // kk = overfetch * k approximate candidates per query and split, then the
@@ -690,13 +874,14 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
     kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
     int kk = int(kk64);
     int cs = 0, stages = 0;
-    while (kk > take && !ssg::stream_choose(kk, &cs, &stages)) --kk;
-    if (!ssg::stream_choose(kk, &cs, &stages))
+    const int heap_rows = ssg::stream_heap_rows(m);
+    while (kk > take && !ssg::stream_choose(kk, heap_rows, &cs, &stages)) --kk;
+    if (!ssg::stream_choose(kk, heap_rows, &cs, &stages))
         return fail(idx, SSG_EUNSUPPORTED, "k = %d does not fit the tensor-core kernel's on-chip top-k", take);
     const int64_t qtiles = (m + 127) / 128;
     const int64_t n_tiles = ssg::tc_tiles(idx->n);
     int64_t splits = idx->splits_param > 0 ? idx->splits_param
-                                           : (ssg::device_sm_count() + qtiles - 1) / qtiles;
+                                           : wave_splits(qtiles, ssg::device_sm_count(), n_tiles);
     splits = std::min<int64_t>(splits, n_tiles);
     splits = std::max<int64_t>(1, splits);
     const int segs = int(splits) * cs;
@@ -729,7 +914,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
         SSG_CK(ssg::launch_stream_scan(qt + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->st_db.p),
                                        static_cast<const float *>(idx->st_alpha.p),
                                        static_cast<const float *>(idx->st_beta.p), qgamma ? qgamma + c0 : nullptr,
-                                       idx->n, mc, idx->dim, fp8, kk, int(splits),
+                                       idx->n, mc, idx->dim, fp8, kk, int(splits), heap_rows,
                                        static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
                                        idx->stream, &idx->last_launches, nullptr),
                "launching the tensor-core scan kernel");
@@ -1147,7 +1332,7 @@ int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t ep
         return fail(idx, SSG_EUNSUPPORTED, "the learned shortlist is for float metrics");
     if (idx->n < 32) return fail(idx, SSG_EINVAL, "the index needs at least 32 objects to train on");
     if (sample_n < 12 || triplets < 0 || epochs < 0 || hidden < 0 || hidden > 8192 || out_dim < 1 ||
-        out_dim > 1024 || batch < 1 || batch > 65536 || !(lr > 0.0))
+        out_dim > 256 || batch < 1 || batch > 65536 || !(lr > 0.0))
         return fail(idx, SSG_EINVAL, "invalid training arguments");
     ssg::TrainArgs t{};
     t.sample = sample_n;
@@ -1225,7 +1410,8 @@ void ssg_destroy(ssg_index *idx) {
                       &idx->red[0], &idx->red[1]})
         b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
-                      &idx->fb_cand})
+                      &idx->fb_cand, &idx->fb_qn, &idx->tc_smp, &idx->tc_smp_norm, &idx->f_out, &idx->f_cnt,
+                      &idx->f_thr})
         b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);

@@ -217,6 +217,9 @@ cudaError_t launch_gemm_t(const ScanArgs &a, const float *db, const float *xaux,
 
 bool gemm_fits(int kk) { return GemmSmem::total(kk) <= size_t(220) * 1024; }
 
+// resident CTAs per SM (the kernel is bounded to 2; shared memory may allow 1)
+int gemm_ctas_per_sm(int kk) { return GemmSmem::total(kk) + 1024 <= size_t(114) * 1024 ? 2 : 1; }
+
 cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
                             const float *q_norm, cudaStream_t st, int *launches) {
     if (!gemm_fits(a.kk)) return cudaErrorInvalidValue;

@@ -110,6 +110,17 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out);
+// Threshold-filter scan for candidate counts beyond the on-chip heaps: every
+// (query, row) with d~ <= thr[query] is appended to the query's fcap-key list.
+cudaError_t launch_tc_filter(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                             int64_t n, int64_t m, int64_t dim, int splits, const float *thr, uint64_t *fout,
+                             int *fcount, int fcap, int *err, cudaStream_t st, int *launches);
+// thr[q] = min over segments of the segment's kk-th key distance.
+cudaError_t launch_sample_bound(const uint64_t *cand, int64_t m, int segs, int kk, float *thr, cudaStream_t st,
+                                int *launches);
+// Sorted first kk filtered keys per query; short or overflowed lists flagged.
+cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_t m, int fcap, int kk,
+                                 uint64_t *cand, int *flags, int *flag_count, cudaStream_t st, int *launches);
 // Merge + exact FP32 rerank of the candidates + (distance, id) sort + decode.
 cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const float *db, const float *db_norm,
                                    int64_t dim, const float *q, const float *q_norm, cudaStream_t st,
@@ -118,7 +129,8 @@ cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const floa
 // ---- K-streaming tensor-core path for any dimension, BF16 or FP8 (tc_stream.cu) ----
 int stream_kbytes(int64_t dim, int fp8);          // padded bytes per row
 size_t stream_tile_bytes(int64_t dim, int fp8);   // bytes per 128-row tile
-bool stream_choose(int kk, int *cs, int *stages);
+int stream_heap_rows(int64_t m);                  // query rows of a tile that own heaps
+bool stream_choose(int kk, int heap_rows, int *cs, int *stages);
 // rows -> K-block tiles; FP8 also writes the per-row scale (scale may be null for BF16)
 cudaError_t launch_stream_tiles(const float *x, int64_t rows, int64_t dim, int fp8, int64_t tiles, uint8_t *out,
                                 float *scale, cudaStream_t st, int *launches);
@@ -127,11 +139,13 @@ cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_
                                 const float *scale, float *alpha, float *beta, cudaStream_t st, int *launches);
 cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, const float *alpha, const float *beta,
                                const float *qgamma, int64_t n, int64_t m, int64_t dim, int fp8, int kk, int splits,
-                               uint64_t *cand, int *err, cudaStream_t st, int *launches, int *segs_per_split);
+                               int heap_rows, uint64_t *cand, int *err, cudaStream_t st, int *launches,
+                               int *segs_per_split);
 
 // ---- plain FP32 GEMM-form scan (gemm_f32.cu) ----
 // Writes `splits` sorted segments of kk keys per query.
 bool gemm_fits(int kk);
+int gemm_ctas_per_sm(int kk);
 cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
                             const float *q_norm, cudaStream_t st, int *launches);
 

@@ -7,8 +7,8 @@
 // exact allknn over a seeded sample of the database, and the triplet loss
 // max(0, |f(a)-f(p)|^2 - |f(a)-f(n)|^2 + margin) is minimised with Adam on
 // FP32 master weights (forward / backward kernels in mlp.cu).  After
-// training every database row is embedded and indexed by a plain FP32 SqL2
-// index of dimension E.  A learned search embeds the queries, shortlists the
+// training every database row is embedded and indexed by a BF16 SqL2 index of
+// dimension E (tensor-core scan).  A learned search embeds the queries, shortlists the
 // S nearest embeddings, re-scores those S candidates with the exact FP32
 // distance of the parent index and keeps the k best.  The recall of that
 // pipeline against the plain method is estimated at training time on held-out
@@ -134,7 +134,11 @@ int learned_index_db(LearnedModel *m, const IndexView &v, std::string &err) {
     if (rc == SSG_OK) {
         if (m->sub) ssg_destroy(m->sub);
         m->sub = nullptr;
-        rc = ssg_create_device(SSG_METRIC_SQL2, SSG_ELEM_F32, m->E, v.n, Z, m->E, SSG_PREC_FP32, &m->sub);
+        // BF16 tensor-core scan of the embeddings; long shortlists take its
+        // threshold-filter path, the exact FP32 rerank in the parent's space
+        // follows in learned_search
+        rc = ssg_create_device(SSG_METRIC_SQL2, SSG_ELEM_F32, m->E, v.n, Z, m->E, SSG_PREC_BF16, &m->sub);
+        if (!rc) rc = ssg_set_param(m->sub, "overfetch", 1.0);
         if (rc) {
             char buf[256];
             ssg_last_error(nullptr, buf, sizeof buf);
@@ -382,7 +386,7 @@ int learned_load(const IndexView &v, const char *path, LearnedModel **out, std::
         err = "not a model file";
         return SSG_EINVAL;
     }
-    if (hdr[0] != v.dim || hdr[1] < 0 || hdr[2] <= 0 || hdr[1] > 65536 || hdr[2] > 4096) {
+    if (hdr[0] != v.dim || hdr[1] < 0 || hdr[2] <= 0 || hdr[1] > 8192 || hdr[2] > 256) {
         fclose(f);
         err = "the model's input dimension does not match the index";
         return SSG_EINVAL;

@@ -35,16 +35,23 @@ __global__ void __launch_bounds__(256) mlp_gemm_kernel(const float *__restrict__
     const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
     float acc[4][4] = {};
     for (int k0 = 0; k0 < K; k0 += GK) {
+        // consecutive threads walk the operand's contiguous dimension: K for
+        // a row-major operand, the rows for a transposed one (coalesced)
         for (int e = tid; e < GK * GT; e += 256) {
-            const int kk = e % GK, r = e / GK;
-            const int gm = m0 + r, gk = k0 + kk;
-            float va = 0.0f;
-            if (gm < M && gk < K) va = ta ? A[size_t(gk) * M + gm] : A[size_t(gm) * K + gk];
-            sA[kk][r] = round_bf16(va, bf16);
-            const int gn = n0 + r;
-            float vb = 0.0f;
-            if (gn < N && gk < K) vb = tb ? B[size_t(gk) * N + gn] : B[size_t(gn) * K + gk];
-            sB[kk][r] = round_bf16(vb, bf16);
+            {
+                const int kk = ta ? e / GT : e % GK, r = ta ? e % GT : e / GK;
+                const int gm = m0 + r, gk = k0 + kk;
+                float va = 0.0f;
+                if (gm < M && gk < K) va = ta ? A[size_t(gk) * M + gm] : A[size_t(gm) * K + gk];
+                sA[kk][r] = round_bf16(va, bf16);
+            }
+            {
+                const int kk = tb ? e / GT : e % GK, r = tb ? e % GT : e / GK;
+                const int gn = n0 + r, gk = k0 + kk;
+                float vb = 0.0f;
+                if (gn < N && gk < K) vb = tb ? B[size_t(gk) * N + gn] : B[size_t(gn) * K + gk];
+                sB[kk][r] = round_bf16(vb, bf16);
+            }
         }
         __syncthreads();
 #pragma unroll

@@ -124,6 +124,13 @@ struct TcArgs {
     int64_t n_tiles;
     uint64_t *cand;
     int *err;
+    // threshold-filter mode (candidate counts beyond the on-chip heaps): every
+    // candidate with d~ <= thr[query] is appended to the query's list of fcap
+    // keys; fcount[query] counts them all (also those past fcap)
+    const float *thr;
+    uint64_t *fout;
+    int *fcount;
+    int fcap;
 };
 
 template <int QT, int STAGES>
@@ -135,7 +142,7 @@ struct TcSmem {
     static size_t total(int kp, int kk) { return 1024 + a_bytes(kp) + b_bytes(kp) + heap_bytes(kk) + bar_bytes(); }
 };
 
-template <int QT, int STAGES, int MC>
+template <int QT, int STAGES, int MC, bool FILTER>
 __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) {
     constexpr int CS = col_splits<QT>();
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -250,14 +257,14 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         constexpr int CHUNKS = TILE / 32 / CS;  // 32-column chunks per warp and tile
         uint64_t *heap = heap_base + (e * 32 + lane);
         uint64_t *cbuf = buf_base + (e * 32 + lane);
-        Heap{heap, a.kk, hs}.init();
+        if (!FILTER) Heap{heap, a.kk, hs}.init();
         // padding rows of a partial query tile filter everything out (a
         // -inf threshold), and warps holding only padding rows skip the
         // epilogue: they just hand the accumulator back
         const bool qvalid = query < a.m;
         const bool warp_live = __any_sync(0xffffffffu, qvalid);
         uint64_t top = KEY_EMPTY;
-        float topd = qvalid ? INFINITY : -INFINITY;
+        float topd = qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
         int nbuf = 0;
         for (int t = 0; t < T_tiles; ++t) {
             const int b = t & 1;
@@ -306,6 +313,20 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                     gmin[g] = MC == MC_DOT ? -m : m;
                 }
                 const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+                if (FILTER) {
+                    // rare: ~3 * kk of the n columns pass a query's threshold
+                    if (__any_sync(0xffffffffu, dmin <= topd)) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const float d = MC == MC_DOT ? -dv[j] : dv[j];
+                            if (d <= topd && id0 + j < a.n) {
+                                const int pos = atomicAdd(a.fcount + query, 1);
+                                if (pos < a.fcap) a.fout[size_t(query) * a.fcap + pos] = make_key(d, uint32_t(id0 + j));
+                            }
+                        }
+                    }
+                    continue;
+                }
                 if (__any_sync(0xffffffffu, dmin <= topd)) {
 #pragma unroll
                     for (int g = 0; g < 4; ++g) {
@@ -327,9 +348,9 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                 }
             }
         }
-        top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        if (!FILTER) top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
         Heap H{heap, a.kk, hs};
-        if (query < a.m) {
+        if (!FILTER && query < a.m) {
             H.sort_ascending();
             uint64_t *out = a.cand + ((size_t(query) * a.splits + blockIdx.y) * CS + cs) * a.kk;
             for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
@@ -343,10 +364,10 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
     }
 }
 
-template <int QT, int STAGES, int MC>
+template <int QT, int STAGES, int MC, bool FILTER>
 cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
     const size_t smem = TcSmem<QT, STAGES>::total(a.kp, a.kk);
-    auto kern = tc_scan_kernel<QT, STAGES, MC>;
+    auto kern = tc_scan_kernel<QT, STAGES, MC, FILTER>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + QT * TILE - 1) / (QT * TILE)), unsigned(a.splits));
@@ -354,11 +375,51 @@ cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-template <int QT, int STAGES>
+template <int QT, int STAGES, bool FILTER = false>
 cudaError_t launch_tc_mc(const TcArgs &a, int mc, cudaStream_t st) {
-    if (mc == MC_SQ) return launch_tc_t<QT, STAGES, MC_SQ>(a, st);
-    if (mc == MC_COS) return launch_tc_t<QT, STAGES, MC_COS>(a, st);
-    return launch_tc_t<QT, STAGES, MC_DOT>(a, st);
+    if (mc == MC_SQ) return launch_tc_t<QT, STAGES, MC_SQ, FILTER>(a, st);
+    if (mc == MC_COS) return launch_tc_t<QT, STAGES, MC_COS, FILTER>(a, st);
+    return launch_tc_t<QT, STAGES, MC_DOT, FILTER>(a, st);
+}
+
+// thr[q] = the smallest over the query's segments of the segment's last
+// (kk-th) key distance: a bound with at least kk sample candidates below it.
+__global__ void sample_bound_kernel(const uint64_t *__restrict__ cand, int64_t m, int segs, int kk,
+                                    float *__restrict__ thr) {
+    const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    float b = INFINITY;
+    for (int s = 0; s < segs; ++s) {
+        const uint64_t key = cand[(size_t(q) * segs + s) * kk + kk - 1];
+        if (key != KEY_EMPTY) b = fminf(b, key_dist(key));
+    }
+    thr[q] = b;
+}
+
+// Per query: sorts the filtered keys and keeps the first kk (sorted); a query
+// whose list holds fewer than kk keys or overflowed is flagged for the exact
+// fallback (its row is filled with empty keys).
+__global__ void filter_select_kernel(const uint64_t *__restrict__ fout, const int *__restrict__ fcount, int fcap,
+                                     int kk, uint64_t *__restrict__ cand, int *__restrict__ flags,
+                                     int *__restrict__ flag_count) {
+    extern __shared__ uint64_t sk[];
+    const int64_t q = blockIdx.x;
+    const int cnt = fcount[q];
+    uint64_t *out = cand + size_t(q) * kk;
+    if (cnt < kk || cnt > fcap) {
+        for (int i = threadIdx.x; i < kk; i += blockDim.x) out[i] = KEY_EMPTY;
+        if (threadIdx.x == 0) {
+            flags[q] = 1;
+            atomicAdd(flag_count, 1);
+        }
+        return;
+    }
+    int P = 1;
+    while (P < cnt) P <<= 1;
+    const uint64_t *src = fout + size_t(q) * fcap;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) sk[i] = i < cnt ? src[i] : KEY_EMPTY;
+    block_bitonic_sort(sk, P);
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) out[i] = sk[i];
 }
 
 constexpr size_t kMaxSmem = 227 * 1024;
@@ -401,6 +462,50 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
     const int mc = metric_class(metric);
     if (launches) *launches += 1;
     tc_norm_kernel<<<unsigned((padded + 255) / 256), 256, 0, st>>>(x, rows, int(dim), padded, mc, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_filter(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                             int64_t n, int64_t m, int64_t dim, int splits, const float *thr, uint64_t *fout,
+                             int *fcount, int fcap, int *err, cudaStream_t st, int *launches) {
+    TcArgs a{};
+    a.qt = q_tiles;
+    a.dt = d_tiles;
+    a.dnorm = d_norm;
+    a.n = n;
+    a.m = m;
+    a.kp = tc_padded_k(dim);
+    a.kk = 0;
+    a.splits = splits;
+    a.n_tiles = tc_tiles(n);
+    a.split_tiles = (a.n_tiles + splits - 1) / splits;
+    a.err = err;
+    a.thr = thr;
+    a.fout = fout;
+    a.fcount = fcount;
+    a.fcap = fcap;
+    if (TcSmem<1, 4>::total(a.kp, 0) > kMaxSmem) return cudaErrorInvalidValue;
+    if (launches) *launches += 1;
+    return launch_tc_mc<1, 4, true>(a, metric_class(metric), st);
+}
+
+cudaError_t launch_sample_bound(const uint64_t *cand, int64_t m, int segs, int kk, float *thr, cudaStream_t st,
+                                int *launches) {
+    if (m <= 0) return cudaSuccess;
+    if (launches) *launches += 1;
+    sample_bound_kernel<<<unsigned((m + 255) / 256), 256, 0, st>>>(cand, m, segs, kk, thr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_t m, int fcap, int kk,
+                                 uint64_t *cand, int *flags, int *flag_count, cudaStream_t st, int *launches) {
+    if (m <= 0) return cudaSuccess;
+    const size_t smem = size_t(next_pow2(fcap)) * 8;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(filter_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    if (launches) *launches += 1;
+    filter_select_kernel<<<unsigned(m), 256, smem, st>>>(fout, fcount, fcap, kk, cand, flags, flag_count);
     return cudaGetLastError();
 }
 

@@ -120,15 +120,21 @@ struct StreamArgs {
     int kblocks;                   // K-blocks per tile
     int fp8;
     int kk, splits;
+    int heap_rows;                 // query rows of a tile that own heaps (32..128)
     int64_t split_tiles, n_tiles;
     uint64_t *cand;
     int *err;
 };
 
+// Heaps exist for the first heap_rows rows of the query tile only: a batch of
+// m < 128 queries leaves the rest of its single tile as padding, and the
+// shared memory saved goes to deeper copy pipelines.
 template <int CS, int STAGES>
 struct StreamSmem {
-    static size_t heap_bytes(int kk) { return size_t(TILE) * CS * (kk + kBufCap) * 8; }
-    static size_t total(int kk) { return 1024 + size_t(STAGES) * 2 * KBLOCK_BYTES + heap_bytes(kk) + 256; }
+    static size_t heap_bytes(int kk, int rows) { return size_t(rows) * CS * (kk + kBufCap) * 8; }
+    static size_t total(int kk, int rows) {
+        return 1024 + size_t(STAGES) * 2 * KBLOCK_BYTES + heap_bytes(kk, rows) + 256;
+    }
 };
 
 template <int CS, int STAGES>
@@ -137,8 +143,8 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sAB = smem;  // [STAGES][A | B]
     uint64_t *heap_base = reinterpret_cast<uint64_t *>(sAB + size_t(STAGES) * 2 * KBLOCK_BYTES);
-    uint64_t *buf_base = heap_base + size_t(TILE) * CS * a.kk;
-    uint64_t *bars = buf_base + size_t(TILE) * CS * kBufCap;
+    uint64_t *buf_base = heap_base + size_t(a.heap_rows) * CS * a.kk;
+    uint64_t *bars = buf_base + size_t(a.heap_rows) * CS * kBufCap;
     uint64_t *full = bars;
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
@@ -235,17 +241,17 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
         const int quarter = warp % 4;
         const int row = quarter * 32 + lane;
         const int64_t query = int64_t(blockIdx.x) * TILE + row;
-        constexpr int hs = TILE * CS;
+        const int hs = a.heap_rows * CS;
         constexpr int CHUNKS = TILE / 32 / CS;
         const float gamma = (a.qgamma && query < a.m) ? a.qgamma[query] : 1.0f;
-        uint64_t *heap = heap_base + (e * 32 + lane);
-        uint64_t *cbuf = buf_base + (e * 32 + lane);
-        Heap{heap, a.kk, hs}.init();
         // padding rows of a partial query tile filter everything out (a
         // -inf threshold), and warps holding only padding rows skip the
-        // epilogue: they just hand the accumulator back
+        // epilogue: they just hand the accumulator back (they own no heap)
         const bool qvalid = query < a.m;
-        const bool warp_live = __any_sync(0xffffffffu, qvalid);
+        const bool warp_live = quarter * 32 < a.heap_rows && __any_sync(0xffffffffu, qvalid);
+        uint64_t *heap = heap_base + (cs * a.heap_rows + quarter * 32 + lane);
+        uint64_t *cbuf = buf_base + (cs * a.heap_rows + quarter * 32 + lane);
+        if (warp_live) Heap{heap, a.kk, hs}.init();
         uint64_t top = KEY_EMPTY;
         float topd = qvalid ? INFINITY : -INFINITY;
         int nbuf = 0;
@@ -309,9 +315,9 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                 }
             }
         }
-        top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        if (warp_live) top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
         Heap H{heap, a.kk, hs};
-        if (query < a.m) {
+        if (warp_live && query < a.m) {
             H.sort_ascending();
             uint64_t *out = a.cand + ((size_t(query) * a.splits + blockIdx.y) * CS + cs) * a.kk;
             for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
@@ -329,7 +335,7 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 template <int CS, int STAGES>
 cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st) {
-    const size_t smem = StreamSmem<CS, STAGES>::total(a.kk);
+    const size_t smem = StreamSmem<CS, STAGES>::total(a.kk, a.heap_rows);
     auto kern = tc_stream_kernel<CS, STAGES>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -346,13 +352,18 @@ int stream_kbytes(int64_t dim, int fp8) {
 }
 size_t stream_tile_bytes(int64_t dim, int fp8) { return size_t(TILE) * stream_kbytes(dim, fp8); }
 
-// (column splits, stages) for kk candidates, or false.
-bool stream_choose(int kk, int *cs, int *stages) {
-    if (StreamSmem<2, 4>::total(kk) <= kMaxSmem) { *cs = 2; *stages = 4; return true; }
-    if (StreamSmem<2, 3>::total(kk) <= kMaxSmem) { *cs = 2; *stages = 3; return true; }
-    if (StreamSmem<1, 4>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 4; return true; }
-    if (StreamSmem<1, 3>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 3; return true; }
-    if (StreamSmem<1, 2>::total(kk) <= kMaxSmem) { *cs = 1; *stages = 2; return true; }
+int stream_heap_rows(int64_t m) { return m >= TILE ? TILE : int((m + 31) / 32 * 32); }
+
+// (column splits, stages) for kk candidates and heap_rows rows with heaps, or
+// false.  Deeper pipelines first (small batches are bound by HBM latency),
+// then two epilogue warps per lane quarter.
+bool stream_choose(int kk, int heap_rows, int *cs, int *stages) {
+    if (StreamSmem<2, 6>::total(kk, heap_rows) <= kMaxSmem) { *cs = 2; *stages = 6; return true; }
+    if (StreamSmem<2, 4>::total(kk, heap_rows) <= kMaxSmem) { *cs = 2; *stages = 4; return true; }
+    if (StreamSmem<2, 3>::total(kk, heap_rows) <= kMaxSmem) { *cs = 2; *stages = 3; return true; }
+    if (StreamSmem<1, 4>::total(kk, heap_rows) <= kMaxSmem) { *cs = 1; *stages = 4; return true; }
+    if (StreamSmem<1, 3>::total(kk, heap_rows) <= kMaxSmem) { *cs = 1; *stages = 3; return true; }
+    if (StreamSmem<1, 2>::total(kk, heap_rows) <= kMaxSmem) { *cs = 1; *stages = 2; return true; }
     return false;
 }
 
@@ -378,7 +389,8 @@ cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_
 
 cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, const float *alpha, const float *beta,
                                const float *qgamma, int64_t n, int64_t m, int64_t dim, int fp8, int kk, int splits,
-                               uint64_t *cand, int *err, cudaStream_t st, int *launches, int *segs_per_split) {
+                               int heap_rows, uint64_t *cand, int *err, cudaStream_t st, int *launches,
+                               int *segs_per_split) {
     StreamArgs a{};
     a.qt = q_tiles;
     a.dt = d_tiles;
@@ -395,11 +407,16 @@ cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, c
     a.split_tiles = (a.n_tiles + splits - 1) / splits;
     a.cand = cand;
     a.err = err;
+    if (heap_rows < stream_heap_rows(m) || heap_rows > TILE || heap_rows % 32) return cudaErrorInvalidValue;
+    a.heap_rows = heap_rows;
     int cs = 0, stages = 0;
-    if (!stream_choose(kk, &cs, &stages)) return cudaErrorInvalidValue;
+    if (!stream_choose(kk, a.heap_rows, &cs, &stages)) return cudaErrorInvalidValue;
     if (segs_per_split) *segs_per_split = cs;
     if (launches) *launches += 1;
-    if (cs == 2) return stages == 4 ? launch_stream_t<2, 4>(a, st) : launch_stream_t<2, 3>(a, st);
+    if (cs == 2) {
+        if (stages == 6) return launch_stream_t<2, 6>(a, st);
+        return stages == 4 ? launch_stream_t<2, 4>(a, st) : launch_stream_t<2, 3>(a, st);
+    }
     if (stages == 4) return launch_stream_t<1, 4>(a, st);
     if (stages == 3) return launch_stream_t<1, 3>(a, st);
     return launch_stream_t<1, 2>(a, st);

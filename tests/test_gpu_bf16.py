@@ -123,3 +123,44 @@ def test_bf16_rejects_hamming(ss):
     B = np.zeros((10, 2), dtype=np.uint64)
     with pytest.raises(ss._native.UnsupportedError):
         ss.GPUExhaustiveSearch(ss.Dist.Bits.Hamming(), ss.MatrixDatabase.from_rows(B), precision="bf16")
+
+
+@pytest.mark.parametrize("name", ["sql2", "cosine", "ip"])
+@pytest.mark.parametrize("n,k", [(30000, 200), (6000, 300)])
+def test_bf16_large_k_threshold_filter(ss, name, n, k):
+    # k beyond the on-chip heaps: the sampled-bound filter path (n > 8192) or
+    # the every-row path (n <= 8192), then the exact rerank
+    rng = np.random.default_rng(n + k + len(name))
+    X = mixture(rng, n, 64, normalise=False)
+    Q = X[rng.integers(0, n, size=150)] + rng.standard_normal((150, 64), dtype=np.float32) * 0.05
+    gi, gd = run(ss, name, X, Q, k, overfetch=1.5)
+    check_reported_distances_exact(name, X, Q[:10], gi[:10], gd[:10])
+    fi, _ = O.searchbatch_f64(name, X, Q, k)
+    assert O.macrorecall(fi, gi) >= 0.99
+
+
+def test_bf16_filter_overflow_falls_back_to_exact_scan(ss):
+    # all rows equal: every distance ties, every row passes the bound, the
+    # filtered lists overflow and each query is recomputed by the exact scan
+    rng = np.random.default_rng(3)
+    X = np.tile(rng.standard_normal((1, 48), dtype=np.float32), (20000, 1))
+    Q = rng.standard_normal((9, 48), dtype=np.float32)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.0)
+    ids, dists = ss.searchbatch(idx, ss.GenericContext(), ss.MatrixDatabase.from_rows(Q), 100)
+    assert idx.get_param("fallbacks") == 9
+    ri, rd = O.searchbatch("sql2", X, Q, 100)
+    assert np.array_equal(np.ascontiguousarray(ids.T), ri) and np.array_equal(np.ascontiguousarray(dists.T), rd)
+
+
+def test_bf16_allknn_large_k(ss):
+    rng = np.random.default_rng(17)
+    X = mixture(rng, 12000, 32)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.NormCosine(), ss.MatrixDatabase.from_rows(X), precision="bf16",
+                                 overfetch=1.5)
+    ids, _ = ss.allknn(idx, ss.GenericContext(), 120, exclude_self=True)
+    gi = np.ascontiguousarray(ids.T)
+    assert not np.any(gi == np.arange(1, 12001, dtype=np.uint32)[:, None])
+    rows = rng.choice(12000, size=60, replace=False)
+    fi, _ = O.searchbatch_f64("normcosine", X, X[rows], 121)
+    gold = np.array([[i for i in fi[r] if i != j + 1][:120] for r, j in enumerate(rows)], dtype=np.uint32)
+    assert O.macrorecall(gold, gi[rows]) >= 0.99

@@ -94,7 +94,7 @@ def test_streaming_full_overfetch_equals_plain(ss, precision):
     assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
 
 
-@pytest.mark.parametrize("m", [1, 129, 700])
+@pytest.mark.parametrize("m", [1, 40, 129, 700])
 @pytest.mark.parametrize("k", [1, 10, 100])
 def test_fp8_batch_sizes_and_k(ss, m, k):
     rng = np.random.default_rng(m * 13 + k)
