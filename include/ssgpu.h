@@ -100,6 +100,21 @@ int ssg_search(ssg_index *idx, const void *host_q, int64_t dim, int64_t m, int32
 int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k,
                       uint32_t *dev_ids, float *dev_dists, int32_t flags);
 
+/* Runs nb query batches of different sizes and k as one search: batch b has
+ * m[b] queries at dev_q[b] (device rows of dim elements of the index's type)
+ * and receives m[b] rows of k[b] results at dev_ids[b] / dev_dists[b] (device
+ * memory).  The arrays themselves are host arrays of nb entries.  All batches
+ * share the query tiles and one scan of the database with the candidates of
+ * the largest k; batch b's rows are the first k[b] entries of that search
+ * (for the plain method exactly the rows of a separate call; for BF16/FP8 a
+ * candidate list at least as long).  Batches with m[b] == 0 are skipped.
+ * Replaces per-request searchbatch! calls on a request stream.  With the
+ * reduced-precision scans the device work of a call is replayed from a CUDA
+ * graph when its shape (queries rounded up to 128, largest k) repeats
+ * ("graphs" param, default 1; "graph_replays", "last_graph" readable). */
+int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, const int64_t *m,
+                       const int32_t *k, uint32_t *const *dev_ids, float *const *dev_dists);
+
 /* All-vs-all k-NN over the indexed objects.  exclude_self == 0 keeps each
  * object in its own result like allknn! (src/allknn.jl:66-110); exclude_self
  * != 0 computes k+1 neighbours and drops the object itself (or the last one
@@ -126,7 +141,8 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * the plain GEMM-form scan, 0 = auto), "exact_scan" (1 = plain method through
  * the direct difference-form scan only), "plain" (1 = plain FP32 method on a
  * BF16/FP8 index, e.g. to calibrate "overfetch" against it), "profile"
- * (1 = time the scan kernel with events).  Unknown keys return SSG_EINVAL. */
+ * (1 = time the scan kernel with events), "graphs" (0 = no CUDA-graph replay
+ * in ssg_search_batches).  Unknown keys return SSG_EINVAL. */
 int ssg_set_param(ssg_index *idx, const char *key, double value);
 /* Readable keys: the tunables plus "n", "dim", "metric", "precision",
  * "main_kernel_ms" / "main_kernel_launches" (accumulated while profiling),

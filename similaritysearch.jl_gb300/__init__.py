@@ -9,7 +9,7 @@ from .db import AbstractDatabase, MatrixDatabase, VectorDatabase
 from .dist import Dist, PreMetric, evaluate
 from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,
                     allknn, allknn_b, append_items_b, database, distance, distance_evaluations, index_b,
-                    push_item_b, rerank_b, search, searchbatch, searchbatch_b)
+                    push_item_b, rerank_b, search, searchbatch, searchbatch_b, searchbatches)
 from .log import LOG, InformativeLog, LogList, RecorderLog
 from .perf import macrorecall, recallscore
 from .pqueue import IdDist, KnnSorted, knnqueue
@@ -23,7 +23,7 @@ __all__ = [
     "ArgumentError", "GenericContext", "GPUExhaustiveSearch", "GPUParallelExhaustiveSearch",
     "add_distance_evaluations", "allknn", "allknn_b", "append_items_b", "database", "distance",
     "distance_evaluations", "index_b", "push_item_b", "rerank_b", "search", "searchbatch",
-    "searchbatch_b", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
+    "searchbatch_b", "searchbatches", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
     "IdDist", "KnnSorted", "knnqueue",
 ]
 

@@ -17,7 +17,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -79,7 +81,8 @@ struct ssg_index {
     DevBuf sq_norm, sq_max, flags, qsq, fb_list, fb_q, fb_out, fb_cand, fb_qn;
     // BF16 threshold-filter path (candidate counts beyond the on-chip heaps):
     // tiles of every smp_r-th database row, filtered lists, counts, bounds
-    DevBuf tc_smp, tc_smp_norm, f_out, f_cnt, f_thr;
+    DevBuf tc_smp, tc_smp_norm, f_out, f_cnt, f_thr, gbound;
+    DevBuf pack_q, pack_out;  // ssg_search_batches staging
     int64_t smp_r = 0, smp_n = -1, smp_rows = 0;
     DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
     // learned shortlist (trained model, whether searches use it, recall target)
@@ -105,6 +108,20 @@ struct ssg_index {
     int64_t main_launches = 0;
     int last_launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // CUDA graphs of ssg_search_batches' device work, one per shape: the
+    // first call of a shape runs eagerly (sizing every buffer), the second is
+    // captured on cap_stream and every later one replays the graph
+    struct GraphEntry {
+        cudaGraphExec_t exec;
+        int launches;
+    };
+    int graphs_param = 1;
+    bool capturing = false;
+    cudaStream_t cap_stream = nullptr;
+    std::map<std::vector<uint64_t>, GraphEntry> graphs;
+    std::set<std::vector<uint64_t>> graph_seen;
+    int64_t graph_replays = 0;
+    int last_graph = 0;
 };
 
 namespace {
@@ -640,12 +657,18 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
 int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                       uint32_t *d_ids, float *d_dists, bool queries_are_db, int kk);
 
+// Candidates kept per query by the reduced-precision scans for `take`
+// neighbours: the over-fetch, at least take, at most max(take, min(n, 4096)).
+int64_t overfetch_kk(const ssg_index *idx, int take) {
+    int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
+    kk64 = std::max<int64_t>(kk64, take);
+    return std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
+}
+
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db) {
     const int take = k + (exclude_self ? 1 : 0);
-    int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
-    kk64 = std::max<int64_t>(kk64, take);
-    kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
+    const int64_t kk64 = overfetch_kk(idx, take);
     const int kp = ssg::tc_padded_k(idx->dim);
     int kk = int(kk64);
     int qt = 0, stages = 0;
@@ -714,6 +737,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
             idx->main_launches += 1;
         }
     }
+    if (idx->capturing) return SSG_OK;  // read after the graph launch
     int status = 0;
     SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
            "reading the status word");
@@ -869,9 +893,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
                    uint32_t *d_ids, float *d_dists, bool queries_are_db) {
     const int fp8 = idx->prec == SSG_PREC_FP8;
     const int take = k + (exclude_self ? 1 : 0);
-    int64_t kk64 = int64_t(idx->overfetch * take + 0.999);
-    kk64 = std::max<int64_t>(kk64, take);
-    kk64 = std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
+    const int64_t kk64 = overfetch_kk(idx, take);
     int kk = int(kk64);
     int cs = 0, stages = 0;
     const int heap_rows = ssg::stream_heap_rows(m);
@@ -907,14 +929,25 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
         qt = static_cast<const uint8_t *>(idx->st_q.p);
         qgamma = qs;
     }
+    // shared per-query bounds pay when many splits fill long heaps of the
+    // same queries (small batches, long candidate lists): with at least kk / 2
+    // heaps per query the checkpoint bounds apply (two best values per heap)
+    uint32_t *gbound = nullptr;
+    if (kk >= 32 && 2 * splits * cs >= kk) {
+        SSG_CK(idx->gbound.ensure(size_t(chunk) * ssg::kBoundWords * 4), "allocating query bounds");
+        gbound = static_cast<uint32_t *>(idx->gbound.p);
+    }
     ScanTimer timer(idx);
     for (int64_t c0 = 0; c0 < m; c0 += chunk) {
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        if (gbound)
+            SSG_CK(cudaMemsetAsync(gbound, 0, size_t(mc) * ssg::kBoundWords * 4, idx->stream),
+                   "clearing query bounds");
         SSG_RC(timer.begin());
         SSG_CK(ssg::launch_stream_scan(qt + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->st_db.p),
                                        static_cast<const float *>(idx->st_alpha.p),
                                        static_cast<const float *>(idx->st_beta.p), qgamma ? qgamma + c0 : nullptr,
-                                       idx->n, mc, idx->dim, fp8, kk, int(splits), heap_rows,
+                                       idx->n, mc, idx->dim, fp8, kk, int(splits), heap_rows, gbound,
                                        static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
                                        idx->stream, &idx->last_launches, nullptr),
                "launching the tensor-core scan kernel");
@@ -935,6 +968,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
                "launching the rerank kernel");
         SSG_RC(timer.collect());
     }
+    if (idx->capturing) return SSG_OK;  // read after the graph launch
     int status = 0;
     SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
            "reading the status word");
@@ -1060,6 +1094,102 @@ int estimate_learned_recall(ssg_index *idx, uint64_t seed) {
     return SSG_OK;
 }
 
+int search_locked(ssg_index *idx, const void *q, int64_t m, int32_t k, uint32_t *ids, float *dists, bool device);
+
+// Whether a search of k neighbours on this index is a fixed sequence of
+// device work with no host decisions (graph-capturable): the reduced-precision
+// scans with on-chip heaps.  The plain method, the BF16 threshold filter and
+// the learned path read flags on the host and run eagerly.
+bool graph_capturable(ssg_index *idx, int k) {
+    if (!idx->graphs_param || idx->profile || idx->plain_param || idx->prec == SSG_PREC_FP32 ||
+        idx->metric == SSG_METRIC_HAMMING || use_learned(idx))
+        return false;
+    if (uses_stream(idx)) return true;
+    int qt = 0, stages = 0;
+    return ssg::tc_choose(ssg::tc_padded_k(idx->dim), int(overfetch_kk(idx, k)), &qt, &stages);
+}
+
+// Everything a captured graph depends on: shape, method, tunables and the
+// device buffers its nodes point at.
+std::vector<uint64_t> graph_key(const ssg_index *idx, int64_t m, int k) {
+    uint64_t of = 0;
+    static_assert(sizeof(double) == 8, "double");
+    memcpy(&of, &idx->overfetch, 8);
+    std::vector<uint64_t> key = {uint64_t(m), uint64_t(k), uint64_t(idx->n), uint64_t(idx->prec),
+                                 uint64_t(idx->metric), of, uint64_t(idx->splits_param)};
+    for (const DevBuf *b : {&idx->db, &idx->db_norm, &idx->tc_db, &idx->tc_norm, &idx->tc_q, &idx->st_db,
+                            &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale, &idx->cand,
+                            &idx->red[0], &idx->red[1], &idx->status, &idx->gbound, &idx->qnorm, &idx->pack_q,
+                            &idx->pack_out})
+        key.push_back(uint64_t(reinterpret_cast<uintptr_t>(b->p)));
+    return key;
+}
+
+void clear_graphs(ssg_index *idx) {
+    for (auto &kv : idx->graphs) cudaGraphExecDestroy(kv.second.exec);
+    idx->graphs.clear();
+    idx->graph_seen.clear();
+}
+
+// search_locked through the graph cache (see ssg_index::graphs), then the
+// status word of the scan.
+int search_graph(ssg_index *idx, const void *q, int64_t m, int32_t k, uint32_t *ids, float *dists) {
+    std::vector<uint64_t> key = graph_key(idx, m, k);
+    auto it = idx->graphs.find(key);
+    if (it == idx->graphs.end()) {
+        const bool seen = idx->graph_seen.count(key) > 0;
+        if (!seen) idx->graph_seen.insert(key);
+        bool captured = false;
+        if (seen) {
+            if (!idx->cap_stream)
+                SSG_CK(cudaStreamCreateWithFlags(&idx->cap_stream, cudaStreamNonBlocking), "creating a stream");
+            // the captured work must follow what is already queued on the index's stream
+            SSG_CK(cudaStreamSynchronize(idx->stream), "draining the stream");
+            cudaStream_t saved = idx->stream;
+            const int launches0 = idx->last_launches;
+            idx->stream = idx->cap_stream;
+            idx->capturing = true;
+            cudaError_t e = cudaStreamBeginCapture(idx->cap_stream, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? search_locked(idx, q, m, k, ids, dists, true) : SSG_OK;
+            cudaGraph_t graph = nullptr;
+            if (e == cudaSuccess) e = cudaStreamEndCapture(idx->cap_stream, &graph);
+            idx->stream = saved;
+            idx->capturing = false;
+            cudaGraphExec_t exec = nullptr;
+            if (rc == SSG_OK && e == cudaSuccess && graph) e = cudaGraphInstantiate(&exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (rc == SSG_OK && e == cudaSuccess && exec && graph_key(idx, m, k) == key) {
+                if (idx->graphs.size() >= 32) clear_graphs(idx);
+                idx->graphs[key] = ssg_index::GraphEntry{exec, idx->last_launches - launches0};
+                it = idx->graphs.find(key);
+                captured = true;
+            } else {
+                // not capturable after all: run it eagerly (which reports
+                // any genuine error of the call)
+                if (exec) cudaGraphExecDestroy(exec);
+                cudaGetLastError();
+                idx->last_launches = launches0;
+            }
+        }
+        if (!captured) {
+            idx->last_graph = 0;
+            int rc = search_locked(idx, q, m, k, ids, dists, true);
+            return rc;
+        }
+    }
+    SSG_CK(cudaGraphLaunch(it->second.exec, idx->stream), "launching a search graph");
+    idx->last_launches += it->second.launches;
+    idx->graph_replays += 1;
+    idx->last_graph = 1;
+    int status = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running a search graph");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the tensor-core scan kernel gave up (code %d)", status);
+    return SSG_OK;
+}
+
 int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t k, uint32_t *ids,
                   float *dists, int32_t flags, bool device) {
     if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
@@ -1078,6 +1208,15 @@ int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t
         for (int64_t i = 0; i < m * int64_t(k); ++i) { ids[i] = 0; dists[i] = INFINITY; }
         return SSG_OK;
     }
+    int rc = search_locked(idx, q, m, k, ids, dists, device);
+    if (rc) return rc;
+    return finish_call(idx, !(device && (flags & 1)));
+}
+
+// The body of a search on a locked, validated index with n > 0: query
+// preparation, the learned path or the index's method, results to the host
+// when !device.  Does not wait for device results.
+int search_locked(ssg_index *idx, const void *q, int64_t m, int32_t k, uint32_t *ids, float *dists, bool device) {
     const void *dq;
     const float *dqn;
     int rc = prepare_queries(idx, q, m, device, &dq, &dqn);
@@ -1105,7 +1244,7 @@ int search_common(ssg_index *idx, const void *q, int64_t dim, int64_t m, int32_t
         SSG_CK(cudaMemcpyAsync(dists, d_dists, size_t(m) * k * 4, cudaMemcpyDeviceToHost, idx->stream),
                "copying distances");
     }
-    return finish_call(idx, !(device && (flags & 1)));
+    return SSG_OK;
 }
 
 int allknn_common(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *ids, float *dists, bool device) {
@@ -1180,6 +1319,65 @@ int ssg_search(ssg_index *idx, const void *host_q, int64_t dim, int64_t m, int32
 int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k, uint32_t *dev_ids,
                       float *dev_dists, int32_t flags) {
     return search_common(idx, dev_q, idx ? idx->dim : 0, m, k, dev_ids, dev_dists, flags, true);
+}
+
+int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, const int64_t *m, const int32_t *k,
+                       uint32_t *const *dev_ids, float *const *dev_dists) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (nb <= 0 || !dev_q || !m || !k || !dev_ids || !dev_dists)
+        return fail(idx, SSG_EINVAL, "need nb > 0 batches and non-NULL arrays");
+    int64_t mt = 0;
+    int32_t kmax = 0;
+    for (int32_t b = 0; b < nb; ++b) {
+        if (m[b] < 0 || k[b] <= 0) return fail(idx, SSG_EINVAL, "batch %d: m must be >= 0 and k > 0", b);
+        if (m[b] > 0 && (!dev_q[b] || !dev_ids[b] || !dev_dists[b]))
+            return fail(idx, SSG_EINVAL, "batch %d: NULL query or output pointer", b);
+        mt += m[b];
+        if (m[b] > 0) kmax = std::max(kmax, k[b]);
+    }
+    if (mt == 0) return SSG_OK;
+    if (idx->n == 0) return fail(idx, SSG_EINVAL, "the index is empty");
+    // pack the batches' queries (one copy each), one search with the largest
+    // k, then each batch's first k columns back to its own output.  Graph
+    // replays need a fixed shape: the packed count is rounded up to whole
+    // 128-query tiles of zero rows.
+    const bool graph = idx->elem == SSG_ELEM_F32 && graph_capturable(idx, kmax);
+    const int64_t mrun = graph ? (mt + 127) / 128 * 128 : mt;
+    const size_t row_bytes = size_t(idx->dim) * elem_size(idx->elem);
+    SSG_CK(idx->pack_q.ensure(size_t(mrun) * row_bytes), "allocating packed queries");
+    SSG_CK(idx->pack_out.ensure(size_t(mrun) * kmax * 8), "allocating packed results");
+    char *pq = static_cast<char *>(idx->pack_q.p);
+    int64_t off = 0;
+    for (int32_t b = 0; b < nb; ++b) {
+        if (m[b] == 0) continue;
+        SSG_CK(cudaMemcpyAsync(pq + size_t(off) * row_bytes, dev_q[b], size_t(m[b]) * row_bytes,
+                               cudaMemcpyDeviceToDevice, idx->stream),
+               "packing queries");
+        off += m[b];
+    }
+    if (mrun > mt)
+        SSG_CK(cudaMemsetAsync(pq + size_t(mt) * row_bytes, 0, size_t(mrun - mt) * row_bytes, idx->stream),
+               "padding packed queries");
+    uint32_t *pi = static_cast<uint32_t *>(idx->pack_out.p);
+    float *pd = reinterpret_cast<float *>(pi + size_t(mrun) * kmax);
+    idx->last_graph = 0;
+    int rc = graph ? search_graph(idx, pq, mrun, kmax, pi, pd) : search_locked(idx, pq, mt, kmax, pi, pd, true);
+    if (rc) return rc;
+    off = 0;
+    for (int32_t b = 0; b < nb; ++b) {
+        if (m[b] == 0) continue;
+        SSG_CK(cudaMemcpy2DAsync(dev_ids[b], size_t(k[b]) * 4, pi + size_t(off) * kmax, size_t(kmax) * 4,
+                                 size_t(std::min(k[b], kmax)) * 4, size_t(m[b]), cudaMemcpyDeviceToDevice,
+                                 idx->stream),
+               "unpacking ids");
+        SSG_CK(cudaMemcpy2DAsync(dev_dists[b], size_t(k[b]) * 4, pd + size_t(off) * kmax, size_t(kmax) * 4,
+                                 size_t(std::min(k[b], kmax)) * 4, size_t(m[b]), cudaMemcpyDeviceToDevice,
+                                 idx->stream),
+               "unpacking distances");
+        off += m[b];
+    }
+    return finish_call(idx, true);
 }
 
 int ssg_allknn(ssg_index *idx, int32_t k, int32_t exclude_self, uint32_t *out_ids, float *out_dists) {
@@ -1260,6 +1458,9 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
             return fail(idx, SSG_EINVAL, "no learned model on this index");
         // the recall estimate belongs to the shortlist length: measure it again
         return estimate_learned_recall(idx, 12345);
+    } else if (k == "graphs") {
+        idx->graphs_param = value != 0.0;
+        if (!idx->graphs_param) clear_graphs(idx);
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -1280,6 +1481,9 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "splits") *value = idx->splits_param;
     else if (k == "overfetch") *value = idx->overfetch;
     else if (k == "profile") *value = idx->profile;
+    else if (k == "graphs") *value = idx->graphs_param;
+    else if (k == "graph_replays") *value = double(idx->graph_replays);
+    else if (k == "last_graph") *value = idx->last_graph;
     else if (k == "main_kernel_ms") *value = idx->main_ms;
     else if (k == "main_kernel_launches") *value = double(idx->main_launches);
     else if (k == "kernel_launches") *value = idx->last_launches;
@@ -1411,10 +1615,12 @@ void ssg_destroy(ssg_index *idx) {
         b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand, &idx->fb_qn, &idx->tc_smp, &idx->tc_smp_norm, &idx->f_out, &idx->f_cnt,
-                      &idx->f_thr})
+                      &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out})
         b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);
+    clear_graphs(idx);
+    if (idx->cap_stream) cudaStreamDestroy(idx->cap_stream);
     if (idx->own_stream && idx->stream) cudaStreamDestroy(idx->stream);
     delete idx;
 }

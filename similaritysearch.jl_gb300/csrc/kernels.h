@@ -129,6 +129,7 @@ cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const floa
 // ---- K-streaming tensor-core path for any dimension, BF16 or FP8 (tc_stream.cu) ----
 int stream_kbytes(int64_t dim, int fp8);          // padded bytes per row
 size_t stream_tile_bytes(int64_t dim, int fp8);   // bytes per 128-row tile
+constexpr int kBoundWords = 16;                   // shared pruning-bound words per query
 int stream_heap_rows(int64_t m);                  // query rows of a tile that own heaps
 bool stream_choose(int kk, int heap_rows, int *cs, int *stages);
 // rows -> K-block tiles; FP8 also writes the per-row scale (scale may be null for BF16)
@@ -139,8 +140,8 @@ cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_
                                 const float *scale, float *alpha, float *beta, cudaStream_t st, int *launches);
 cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, const float *alpha, const float *beta,
                                const float *qgamma, int64_t n, int64_t m, int64_t dim, int fp8, int kk, int splits,
-                               int heap_rows, uint64_t *cand, int *err, cudaStream_t st, int *launches,
-                               int *segs_per_split);
+                               int heap_rows, uint32_t *gbound, uint64_t *cand, int *err, cudaStream_t st,
+                               int *launches, int *segs_per_split);
 
 // ---- plain FP32 GEMM-form scan (gemm_f32.cu) ----
 // Writes `splits` sorted segments of kk keys per query.

@@ -142,6 +142,17 @@ struct TcSmem {
     static size_t total(int kp, int kk) { return 1024 + a_bytes(kp) + b_bytes(kp) + heap_bytes(kk) + bar_bytes(); }
 };
 
+// Epilogue warps of this CTA whose lane quarter holds at least one query: only
+// they take part in the accumulator hand-off; the others leave at once.
+template <int QT, int CS>
+__device__ __forceinline__ int tc_live_warps(const TcArgs &a) {
+    int live = 0;
+    for (int q = 0; q < QT; ++q)
+        for (int w = 0; w < 4; ++w)
+            if ((int64_t(blockIdx.x) * QT + q) * TILE + w * 32 < a.m) live += CS;
+    return live;
+}
+
 template <int QT, int STAGES, int MC, bool FILTER>
 __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) {
     constexpr int CS = col_splits<QT>();
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 4 * QT * CS);
+            tc::mbar_init(&acc_empty[b], tc_live_warps<QT, CS>(a));
         }
         tc::mbar_init(mma_done, 1);
         tc::fence_mbarrier_init();
@@ -262,23 +273,17 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         // -inf threshold), and warps holding only padding rows skip the
         // epilogue: they just hand the accumulator back
         const bool qvalid = query < a.m;
-        const bool warp_live = __any_sync(0xffffffffu, qvalid);
+        const bool warp_live = (int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
         uint64_t top = KEY_EMPTY;
         float topd = qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
         int nbuf = 0;
-        for (int t = 0; t < T_tiles; ++t) {
+        for (int t = 0; warp_live && t < T_tiles; ++t) {
             const int b = t & 1;
             int ok = 1;
             if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 7) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
-            if (!warp_live) {
-                tc::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-                continue;
-            }
             const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
             // this warp's columns in flight together, one wait, then the
             // accumulator goes back to the MMA warp before any filtering

@@ -121,6 +121,9 @@ struct StreamArgs {
     int fp8;
     int kk, splits;
     int heap_rows;                 // query rows of a tile that own heaps (32..128)
+    // per query, kBoundWords zero-initialised words of shared pruning bounds
+    // (SharedBound), nullptr: unused
+    uint32_t *gbound;
     int64_t split_tiles, n_tiles;
     uint64_t *cand;
     int *err;
@@ -129,6 +132,85 @@ struct StreamArgs {
 // Heaps exist for the first heap_rows rows of the query tile only: a batch of
 // m < 128 queries leaves the rest of its single tile as padding, and the
 // shared memory saved goes to deeper copy pipelines.
+// Exact pruning bounds shared by all heaps of a query (every split and column
+// half of it), kBoundWords words per query, zero-initialised:
+//   w[0]      complement of the smallest frontier any full heap reached: that
+//             heap alone holds kk keys at or below it;
+//   w[1 + j]  at checkpoint j (after 2^j tiles), the largest over the heaps
+//             of the c-th best candidate each has seen (c = 1 or 2, all
+//             columns counted, filtered or not): once all heaps have
+//             published it, kk <= c * heaps candidates lie at or below it;
+//   w[8 + j]  how many heaps have published checkpoint j (each publishes its
+//             value, fences, then counts; readers read the count, fence,
+//             then the value).
+// A bound B means the kk-th best approximate distance is <= B, so a
+// candidate with d > B can be dropped: the kept set is unchanged.  Small
+// batches with long candidate lists scan with ~150 splits whose heaps would
+// otherwise each fill up alone; the kernel variant with these bounds
+// (BOUND) is used for them only.
+constexpr int kCheckpoints = 7;
+
+struct SharedBound {
+    uint32_t *w;   // this query's words
+    int nheaps;    // heaps per query
+    int cbest;     // best-seen values tracked per heap (1 or 2), 0: checkpoints off
+    int next_pub, next_read;
+    float b1, b2, cap;
+    uint32_t top_seen;
+
+    __device__ __forceinline__ void init(uint32_t *words, int heaps, int kk) {
+        w = words;
+        nheaps = heaps;
+        const int c = (kk + heaps - 1) / heaps;
+        cbest = c <= 2 ? c : 0;
+        next_pub = next_read = 0;
+        b1 = b2 = cap = INFINITY;
+        top_seen = 0xffffffffu;
+    }
+    // tightens cap from the frontiers and the completed checkpoints
+    __device__ __forceinline__ void refresh() {
+        const uint32_t f = ~__ldcg(w);
+        if (f < top_seen) {
+            top_seen = f;
+            cap = fminf(cap, ordered_to_float(f));
+        }
+        while (cbest && next_read < kCheckpoints) {
+            if (__ldcg(w + 8 + next_read) < uint32_t(nheaps)) break;
+            __threadfence();
+            cap = fminf(cap, ordered_to_float(__ldcg(w + 1 + next_read)));
+            ++next_read;
+        }
+    }
+    // a full heap's frontier
+    __device__ __forceinline__ void frontier(uint64_t top) {
+        const uint32_t o = uint32_t(top >> 32);
+        if (o < top_seen) {
+            top_seen = o;
+            atomicMax(w, ~o);
+            cap = fminf(cap, ordered_to_float(o));
+        }
+    }
+    __device__ __forceinline__ void see(float v) {
+        if (cbest == 1) {
+            b1 = fminf(b1, v);
+        } else {
+            const float n1 = fminf(b1, v);
+            b2 = fminf(b2, fmaxf(b1, v));
+            b1 = n1;
+        }
+    }
+    // publishes the checkpoints reached after `done` tiles (all of them once
+    // the heap's split is finished)
+    __device__ __forceinline__ void checkpoint(int done, bool finished) {
+        while (cbest && next_pub < kCheckpoints && (finished || done >= (1 << next_pub))) {
+            atomicMax(w + 1 + next_pub, float_to_ordered(cbest == 1 ? b1 : b2));
+            __threadfence();
+            atomicAdd(w + 8 + next_pub, 1u);
+            ++next_pub;
+        }
+    }
+};
+
 template <int CS, int STAGES>
 struct StreamSmem {
     static size_t heap_bytes(int kk, int rows) { return size_t(rows) * CS * (kk + kBufCap) * 8; }
@@ -137,7 +219,19 @@ struct StreamSmem {
     }
 };
 
-template <int CS, int STAGES>
+// Epilogue warps of this CTA that own a heap and hold a query: (lane quarter,
+// column half) pairs whose quarter starts below heap_rows and below m.  Only
+// they take part in the accumulator hand-off; the others leave at once
+// instead of spinning on barriers for nothing.
+template <int CS>
+__device__ __forceinline__ int stream_live_warps(const StreamArgs &a) {
+    int live = 0;
+    for (int q = 0; q < 4; ++q)
+        if (q * 32 < a.heap_rows && int64_t(blockIdx.x) * TILE + q * 32 < a.m) live += CS;
+    return live;
+}
+
+template <int CS, int STAGES, bool BOUND>
 __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamArgs a) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -163,7 +257,7 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 4 * CS);
+            tc::mbar_init(&acc_empty[b], stream_live_warps<CS>(a));
         }
         tc::mbar_init(mma_done, 1);
         tc::fence_mbarrier_init();
@@ -248,25 +342,26 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
         // -inf threshold), and warps holding only padding rows skip the
         // epilogue: they just hand the accumulator back (they own no heap)
         const bool qvalid = query < a.m;
-        const bool warp_live = quarter * 32 < a.heap_rows && __any_sync(0xffffffffu, qvalid);
+        const bool warp_live = quarter * 32 < a.heap_rows && int64_t(blockIdx.x) * TILE + quarter * 32 < a.m;
         uint64_t *heap = heap_base + (cs * a.heap_rows + quarter * 32 + lane);
         uint64_t *cbuf = buf_base + (cs * a.heap_rows + quarter * 32 + lane);
         if (warp_live) Heap{heap, a.kk, hs}.init();
         uint64_t top = KEY_EMPTY;
         float topd = qvalid ? INFINITY : -INFINITY;
+        const bool shared = BOUND && qvalid;
+        SharedBound sb;
+        sb.init(shared ? a.gbound + size_t(query) * kBoundWords : nullptr, a.splits * CS, a.kk);
         int nbuf = 0;
-        for (int t = 0; t < T_tiles; ++t) {
+        for (int t = 0; warp_live && t < T_tiles; ++t) {
             const int b = t & 1;
             int ok = 1;
             if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 16) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
-            if (!warp_live) {
-                tc::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-                continue;
+            if (shared) {
+                sb.refresh();
+                topd = fminf(topd, sb.cap);
             }
             const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
             uint32_t r[CHUNKS][32];
@@ -297,6 +392,16 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                     gmin[g] = mn;
                 }
                 const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+                if (shared && sb.cbest) {
+                    // best candidates seen, padding rows of the last tile excluded
+                    if (sb.cbest == 1 && id0 + 32 <= a.n) {
+                        sb.see(dmin);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (id0 + j < a.n) sb.see(dv[j]);
+                    }
+                }
                 if (__any_sync(0xffffffffu, dmin <= topd)) {
 #pragma unroll
                     for (int g = 0; g < 4; ++g) {
@@ -310,11 +415,17 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                             top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
                             nbuf = 0;
                             topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                            if (shared) {
+                                if (top != KEY_EMPTY) sb.frontier(top);
+                                topd = fminf(topd, sb.cap);
+                            }
                         }
                     }
                 }
             }
+            if (shared) sb.checkpoint(t + 1, false);
         }
+        if (shared) sb.checkpoint(T_tiles, true);
         if (warp_live) top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
         Heap H{heap, a.kk, hs};
         if (warp_live && query < a.m) {
@@ -336,7 +447,7 @@ constexpr size_t kMaxSmem = 227 * 1024;
 template <int CS, int STAGES>
 cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st) {
     const size_t smem = StreamSmem<CS, STAGES>::total(a.kk, a.heap_rows);
-    auto kern = tc_stream_kernel<CS, STAGES>;
+    auto kern = a.gbound ? tc_stream_kernel<CS, STAGES, true> : tc_stream_kernel<CS, STAGES, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + TILE - 1) / TILE), unsigned(a.splits));
@@ -389,8 +500,8 @@ cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_
 
 cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, const float *alpha, const float *beta,
                                const float *qgamma, int64_t n, int64_t m, int64_t dim, int fp8, int kk, int splits,
-                               int heap_rows, uint64_t *cand, int *err, cudaStream_t st, int *launches,
-                               int *segs_per_split) {
+                               int heap_rows, uint32_t *gbound, uint64_t *cand, int *err, cudaStream_t st,
+                               int *launches, int *segs_per_split) {
     StreamArgs a{};
     a.qt = q_tiles;
     a.dt = d_tiles;
@@ -409,6 +520,7 @@ cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, c
     a.err = err;
     if (heap_rows < stream_heap_rows(m) || heap_rows > TILE || heap_rows % 32) return cudaErrorInvalidValue;
     a.heap_rows = heap_rows;
+    a.gbound = gbound;
     int cs = 0, stages = 0;
     if (!stream_choose(kk, a.heap_rows, &cs, &stages)) return cudaErrorInvalidValue;
     if (segs_per_split) *segs_per_split = cs;

@@ -245,6 +245,34 @@ def searchbatch(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, k: int, sorted
     return searchbatch_b(idx, ctx, Q, ids, dists, sorted=sorted)
 
 
+def searchbatches(idx: GPUExhaustiveSearch, ctx: GenericContext, Qs, ks):
+    """Several query batches of different sizes and k answered by one search
+    (``ssg_search_batches``): the request-stream form of calling
+    ``searchbatch`` once per request.  Returns one ``(ids (k, m), dists (k, m))``
+    pair per batch.  Device staging goes through torch tensors."""
+    import torch
+    if len(Qs) != len(ks) or not Qs:
+        raise ArgumentError("need one k per batch and at least one batch")
+    qs = [idx._queries(Q) for Q in Qs]
+    host = [q.view(np.int64) if q.dtype == np.uint64 else q for q in qs]   # torch has no uint64 tensors
+    dev_q = [torch.from_numpy(h).cuda() if h.shape[0] else None for h in host]
+    outs_i = [torch.empty((q.shape[0], int(k)), dtype=torch.int32, device="cuda") for q, k in zip(qs, ks)]
+    outs_d = [torch.empty((q.shape[0], int(k)), dtype=torch.float32, device="cuda") for q, k in zip(qs, ks)]
+    nb = len(qs)
+    P = C.c_void_p * nb
+    ptr = lambda t: t.data_ptr() if t is not None and t.numel() else None
+    N.check(N.lib().ssg_search_batches(
+        idx._h, nb, P(*[ptr(t) for t in dev_q]), (C.c_int64 * nb)(*[q.shape[0] for q in qs]),
+        (C.c_int32 * nb)(*[int(k) for k in ks]), P(*[ptr(t) for t in outs_i]), P(*[ptr(t) for t in outs_d])),
+        idx._h)
+    res = []
+    for q, ti, td in zip(qs, outs_i, outs_d):
+        add_distance_evaluations(ctx, q.shape[0] * len(idx))
+        res.append((np.asfortranarray(ti.cpu().numpy().view(np.uint32).T),
+                    np.asfortranarray(td.cpu().numpy().T)))
+    return res
+
+
 def search(idx: GPUExhaustiveSearch, ctx: GenericContext, q, res: AbstractKnnQueue):
     """search(index, ctx, q, res): one query as a batch of one; the results are
     pushed into ``res`` in (distance, id) order (sequential-exhaustive.jl:68-80)."""
