@@ -83,6 +83,10 @@ struct ssg_index {
     // tiles of every smp_r-th database row, filtered lists, counts, bounds
     DevBuf tc_smp, tc_smp_norm, f_out, f_cnt, f_thr, gbound;
     DevBuf pack_q, pack_out;  // ssg_search_batches staging
+    // plain GEMM-form scan: k-major tiles of the database (built for gm_rows
+    // rows) and of the current queries
+    DevBuf gm_db, gm_q;
+    int64_t gm_rows = -1;
     int64_t smp_r = 0, smp_n = -1, smp_rows = 0;
     DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
     // learned shortlist (trained model, whether searches use it, recall target)
@@ -519,12 +523,32 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
                                        std::max<int64_t>(1, idx->n / 512));
     splits = std::min<int64_t>(splits, std::max<int64_t>(1, idx->n / 512));
     splits = std::max<int64_t>(1, splits);
-    const int64_t split_len = (idx->n + splits - 1) / splits;
+    // splits of whole 128-row tiles
+    const int64_t n_tiles = (idx->n + 127) / 128;
+    const int64_t split_len = (n_tiles + splits - 1) / splits * 128;
+    splits = (idx->n + split_len - 1) / split_len;
     const int segs = int(splits);
     const size_t per_query = size_t(segs) * kk * 8;
     int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
     chunk = std::min<int64_t>(chunk, m);
     SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    // k-major operand tiles: the database's (kept until it changes), the queries'
+    const size_t tile_bytes = ssg::gemm_tile_floats(idx->dim) * 4;
+    if (idx->gm_rows != idx->n) {
+        SSG_CK(idx->gm_db.ensure(size_t(n_tiles) * tile_bytes), "allocating database tiles");
+        SSG_CK(ssg::launch_gemm_tiles(static_cast<const float *>(idx->db.p), idx->n, idx->dim, n_tiles,
+                                      static_cast<float *>(idx->gm_db.p), idx->stream, &idx->last_launches),
+               "building database tiles");
+        idx->gm_rows = idx->n;
+    }
+    const float *qtile_base = static_cast<const float *>(idx->gm_db.p);
+    if (dq != idx->db.p) {
+        SSG_CK(idx->gm_q.ensure(size_t(qtiles) * tile_bytes), "allocating query tiles");
+        SSG_CK(ssg::launch_gemm_tiles(dq, m, idx->dim, qtiles, static_cast<float *>(idx->gm_q.p), idx->stream,
+                                      &idx->last_launches),
+               "building query tiles");
+        qtile_base = static_cast<const float *>(idx->gm_q.p);
+    }
     if (sq) {
         SSG_CK(idx->flags.ensure(size_t(m) * 4 + 16), "allocating query flags");
         SSG_CK(idx->qsq.ensure(size_t(chunk) * 4 + 16), "allocating query norms");
@@ -547,8 +571,9 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
         const float *qc = dq + size_t(c0) * idx->dim;
         const float *xaux = sq ? static_cast<const float *>(idx->sq_norm.p) : static_cast<const float *>(idx->db_norm.p);
         SSG_RC(timer.begin());
-        SSG_CK(ssg::launch_gemm_f32(a, static_cast<const float *>(idx->db.p), xaux, qc, dqn ? dqn + c0 : nullptr,
-                                    idx->stream, &idx->last_launches),
+        SSG_CK(ssg::launch_gemm_f32(a, static_cast<const float *>(idx->gm_db.p), xaux,
+                                    qtile_base + size_t(c0 / 128) * ssg::gemm_tile_floats(idx->dim),
+                                    dqn ? dqn + c0 : nullptr, idx->stream, &idx->last_launches),
                "launching the FP32 scan kernel");
         SSG_RC(timer.end());
         ssg::FinalizeArgs f{};
@@ -1615,7 +1640,7 @@ void ssg_destroy(ssg_index *idx) {
         b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand, &idx->fb_qn, &idx->tc_smp, &idx->tc_smp_norm, &idx->f_out, &idx->f_cnt,
-                      &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out})
+                      &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out, &idx->gm_db, &idx->gm_q})
         b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);

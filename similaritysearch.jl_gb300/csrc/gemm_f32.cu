@@ -3,12 +3,14 @@
 // The plain method's fast path.  A CTA computes a 128-query x 128-row tile
 // of dot products with 8x8 accumulators per thread (FFMA, k in index order,
 // so every dot product is the same fma chain as search(::ExhaustiveSearch)'s
-// `d = muladd(a_i, b_i, d)`, src/dist/cos.jl:78-84).  Operand slices of 16
-// dims are copied global -> shared with 4-byte cp.async straight into the
-// k-major layout the inner loop reads (double-buffered), so no registers are
-// spent on staging and two CTAs fit on an SM.  After the last slice the tile
-// is staged in two 64-row halves through the operand buffers; thread r
-// (r < 128) owns query row r and pushes its 128 values into its top-k.
+// `d = muladd(a_i, b_i, d)`, src/dist/cos.jl:78-84).  Database and queries
+// are kept in HBM as k-major tiles (per 128 rows: dim-major, 128 floats per
+// dim, zero-padded), so a slice of BK dims is one contiguous 8 KB block that
+// 16-byte cp.async copies land in shared memory in exactly the layout the
+// inner loop reads (STAGES-deep ring, no registers spent on staging, two
+// CTAs per SM).  After the last slice the tile is staged in two 64-row halves
+// through the operand buffers; thread r (r < 128) owns query row r and pushes
+// its 128 values into its top-k.
 //   * NormCosine / InnerProduct / Cosine: the tile values ARE the exact FP32
 //     distances (1 - dot, -dot, 1 - dot / (|x| |q|)), so the keys are final.
 //   * SqL2 / L2: the tile holds |x|^2 - 2 x.q (the query's |q|^2 is common to
@@ -26,18 +28,26 @@ namespace {
 
 constexpr int BM = 128;       // queries per CTA
 constexpr int BN = 128;       // database rows per tile
-constexpr int BK = 16;        // dims per pipeline stage
-constexpr int LDA = BM + 4;   // padded k-major row (floats)
+#ifndef SSG_GEMM_BK
+#define SSG_GEMM_BK 16
+#endif
+#ifndef SSG_GEMM_STAGES
+#define SSG_GEMM_STAGES 3
+#endif
+constexpr int BK = SSG_GEMM_BK;  // dims per pipeline stage
+constexpr int LDA = BM;       // k-major slice row (floats): the tile layout in HBM
 constexpr int SROW = BN + 4;  // staged tile row stride (floats)
 constexpr int THREADS = 256;
-constexpr int STAGES = 3;         // cp.async pipeline depth (slices in flight)
+constexpr int STAGES = SSG_GEMM_STAGES;  // cp.async ring depth (STAGES - 1 slices in flight ahead)
 constexpr int kBufCap = 12;       // buffered top-k: drain checked every 8 values, trigger 4
 constexpr int kDrainTrigger = 4;
 
-static_assert(STAGES * 2 * BK * LDA >= (BM / 2) * SROW, "a staged half tile must fit the operand buffers");
-
 struct GemmSmem {
-    __host__ __device__ static constexpr size_t operands() { return size_t(STAGES) * 2 * BK * LDA * 4; }
+    // operand ring, also holding a staged half tile in the epilogue
+    __host__ __device__ static constexpr size_t operands() {
+        return size_t(STAGES) * 2 * BK * LDA * 4 > size_t(BM / 2) * SROW * 4 ? size_t(STAGES) * 2 * BK * LDA * 4
+                                                                             : size_t(BM / 2) * SROW * 4;
+    }
     static size_t heaps(int kk) { return size_t(BM) * (kk + kBufCap) * 8; }
     static size_t total(int kk) { return operands() + heaps(kk); }
 };
@@ -50,39 +60,50 @@ __device__ __forceinline__ float gemm_value(float acc, float xaux, float qn) {
     return fmaf(-2.0f, acc, xaux);  // SQL2 / L2: |x|^2 - 2 x.q
 }
 
-__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
     const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
-    const int sz = valid ? 4 : 0;  // src-size 0: the 4 bytes are zero-filled
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-// all but the most recently committed group are complete
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+// all but the STAGES - 2 most recently committed groups are complete
+__device__ __forceinline__ void cp_async_wait_ahead() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(STAGES - 2) : "memory");
+}
 
-// Issues the copies of the k-slice [k0, k0+BK) of 128 rows of `base` into the
-// k-major buffer s (s[k][row]); rows >= rows_valid or dims >= dim are zeros.
-// Thread -> (row = tid / 2, 8 consecutive dims).
-__device__ __forceinline__ void load_slice_async(float *s, const float *__restrict__ base, int64_t row0,
-                                                 int64_t rows_valid, int dim, int k0) {
-    const int tid = threadIdx.x;
-    const int row = tid >> 1;
-    const int c0 = (tid & 1) * 8;
-    const int64_t gr = row0 + row;
-    const bool rv = gr < rows_valid;
-    const float *src = base + (rv ? gr : 0) * dim;
+// Issues the copies of the k-slice [k0, k0+BK) of a k-major tile (BK * 128
+// contiguous floats) into the slice buffer s: 16 bytes per thread and pass.
+__device__ __forceinline__ void load_slice_async(float *s, const float *__restrict__ tile, int k0) {
+    const float *src = tile + size_t(k0) * BM;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const int c = k0 + c0 + i;
-        const bool v = rv && c < dim;
-        cp_async4(s + (c0 + i) * LDA + row, v ? src + c : base, v);
+    for (int i = threadIdx.x; i < BK * BM / 4; i += THREADS) cp_async16(s + i * 4, src + i * 4);
+}
+
+// k-major tiles: out[(t * kpad + k) * 128 + r] = x[(t * 128 + r) * dim + k],
+// zero for rows >= rows or k >= dim.  A block transposes 32 rows x 32 dims
+// through shared memory (coalesced reads and writes).
+__global__ void gemm_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kpad, int64_t tiles,
+                                 float *__restrict__ out) {
+    __shared__ float t[32][33];
+    const int64_t r0 = int64_t(blockIdx.x) * 32;  // row block (within all padded rows)
+    const int k0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t r = r0 + i;
+        const int k = k0 + threadIdx.x;
+        t[i][threadIdx.x] = (r < rows && k < dim) ? x[r * dim + k] : 0.0f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int k = k0 + i;
+        const int64_t r = r0 + threadIdx.x;
+        if (k < kpad && r < tiles * BM) out[((r / BM) * kpad + k) * BM + (r % BM)] = t[threadIdx.x][i];
     }
 }
 
 template <int METRIC>
 __global__ void __launch_bounds__(THREADS, 2)
-gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restrict__ xaux,
-                const float *__restrict__ Q, const float *__restrict__ qn) {
+gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const float *__restrict__ xaux,
+                const float *__restrict__ qtiles, const float *__restrict__ qn) {
     extern __shared__ __align__(16) unsigned char smem[];
     float *sA = reinterpret_cast<float *>(smem);  // [STAGES][BK][LDA]
     float *sB = sA + STAGES * BK * LDA;            // [STAGES][BK][LDA]
@@ -93,9 +114,9 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
     const int64_t q0 = int64_t(blockIdx.x) * BM;
-    const int64_t lo = int64_t(blockIdx.y) * a.split_len;
+    const int64_t lo = int64_t(blockIdx.y) * a.split_len;  // a multiple of BN
     const int64_t hi = lo + a.split_len < a.n ? lo + a.split_len : a.n;
-    const int dim = int(a.dim);
+    const float *qtile = qtiles + size_t(blockIdx.x) * kpad * BM;
 
     // thread r < 128 owns query row r (warps 0-3)
     const bool owner = tid < BM;
@@ -111,23 +132,24 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
             for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 
         __syncthreads();  // the previous tile's epilogue is done with shared memory
-        const int nslices = (dim + BK - 1) / BK;
-        // prologue: slices 0 and 1 in flight (one commit group each, maybe empty)
-        load_slice_async(sA, Q, q0, a.m, dim, 0);
-        load_slice_async(sB, db, j0, hi, dim, 0);
-        cp_async_commit();
-        if (nslices > 1) {
-            load_slice_async(sA + BK * LDA, Q, q0, a.m, dim, BK);
-            load_slice_async(sB + BK * LDA, db, j0, hi, dim, BK);
+        const int nslices = kpad / BK;
+        const float *dtile = dtiles + size_t(j0 / BN) * kpad * BN;
+        // prologue: slices 0 .. STAGES-2 in flight (one commit group each, maybe empty)
+#pragma unroll
+        for (int p = 0; p < STAGES - 1; ++p) {
+            if (p < nslices) {
+                load_slice_async(sA + p * BK * LDA, qtile, p * BK);
+                load_slice_async(sB + p * BK * LDA, dtile, p * BK);
+            }
+            cp_async_commit();
         }
-        cp_async_commit();
         for (int sl = 0; sl < nslices; ++sl) {
-            cp_async_wait_one();
+            cp_async_wait_ahead();
             __syncthreads();  // slice sl visible; the buffer of slice sl-1 is free
-            if (sl + 2 < nslices) {
-                const int nb = (sl + 2) % STAGES;
-                load_slice_async(sA + nb * BK * LDA, Q, q0, a.m, dim, (sl + 2) * BK);
-                load_slice_async(sB + nb * BK * LDA, db, j0, hi, dim, (sl + 2) * BK);
+            if (sl + STAGES - 1 < nslices) {
+                const int nb = (sl + STAGES - 1) % STAGES;
+                load_slice_async(sA + nb * BK * LDA, qtile, (sl + STAGES - 1) * BK);
+                load_slice_async(sB + nb * BK * LDA, dtile, (sl + STAGES - 1) * BK);
             }
             cp_async_commit();
             const int buf = sl % STAGES;
@@ -176,10 +198,15 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
             // warps 2h and 2h+1 own rows [64h, 64h + 64)
             if ((tid >> 6) == h) {
                 const float *row = sT + (tid - h * 64) * SROW;
+                // a group of 8 values is only looked at when one of the warp's
+                // rows may take one of them (padding rows take none)
 #pragma unroll 2
                 for (int c = 0; c < BN; c += 8) {
                     const float4 v0 = *reinterpret_cast<const float4 *>(row + c);
                     const float4 v1 = *reinterpret_cast<const float4 *>(row + c + 4);
+                    const float gm = fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)),
+                                           fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w)));
+                    if (!__any_sync(0xffffffffu, gm <= (row_valid ? T.topd : -INFINITY))) continue;
                     const float vv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -202,14 +229,14 @@ gemm_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restric
 }
 
 template <int METRIC>
-cudaError_t launch_gemm_t(const ScanArgs &a, const float *db, const float *xaux, const float *q, const float *qn,
-                          cudaStream_t st) {
+cudaError_t launch_gemm_t(const ScanArgs &a, int kpad, const float *dtiles, const float *xaux, const float *qtiles,
+                          const float *qn, cudaStream_t st) {
     const size_t smem = GemmSmem::total(a.kk);
     auto kern = gemm_f32_kernel<METRIC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + BM - 1) / BM), unsigned(a.splits));
-    kern<<<grid, THREADS, smem, st>>>(a, db, xaux, q, qn);
+    kern<<<grid, THREADS, smem, st>>>(a, kpad, dtiles, xaux, qtiles, qn);
     return cudaGetLastError();
 }
 
@@ -220,16 +247,30 @@ bool gemm_fits(int kk) { return GemmSmem::total(kk) <= size_t(220) * 1024; }
 // resident CTAs per SM (the kernel is bounded to 2; shared memory may allow 1)
 int gemm_ctas_per_sm(int kk) { return GemmSmem::total(kk) + 1024 <= size_t(114) * 1024 ? 2 : 1; }
 
-cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
+int gemm_kpad(int64_t dim) { return int((dim + BK - 1) / BK * BK); }
+size_t gemm_tile_floats(int64_t dim) { return size_t(gemm_kpad(dim)) * BM; }
+
+cudaError_t launch_gemm_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, float *out, cudaStream_t st,
+                              int *launches) {
+    if (tiles <= 0) return cudaSuccess;
+    const int kpad = gemm_kpad(dim);
+    dim3 grid(unsigned(tiles * BM / 32), unsigned((kpad + 31) / 32));
+    if (launches) *launches += 1;
+    gemm_tile_kernel<<<grid, dim3(32, 8), 0, st>>>(x, rows, int(dim), kpad, tiles, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_f32(const ScanArgs &a, const float *dtiles, const float *xaux, const float *qtiles,
                             const float *q_norm, cudaStream_t st, int *launches) {
-    if (!gemm_fits(a.kk)) return cudaErrorInvalidValue;
+    if (!gemm_fits(a.kk) || a.split_len % BN) return cudaErrorInvalidValue;
+    const int kpad = gemm_kpad(a.dim);
     if (launches) *launches += 1;
     switch (a.metric) {
-        case SQL2: return launch_gemm_t<SQL2>(a, db, xaux, q, q_norm, st);
-        case L2: return launch_gemm_t<L2>(a, db, xaux, q, q_norm, st);
-        case NORMCOSINE: return launch_gemm_t<NORMCOSINE>(a, db, xaux, q, q_norm, st);
-        case COSINE: return launch_gemm_t<COSINE>(a, db, xaux, q, q_norm, st);
-        case IP: return launch_gemm_t<IP>(a, db, xaux, q, q_norm, st);
+        case SQL2: return launch_gemm_t<SQL2>(a, kpad, dtiles, xaux, qtiles, q_norm, st);
+        case L2: return launch_gemm_t<L2>(a, kpad, dtiles, xaux, qtiles, q_norm, st);
+        case NORMCOSINE: return launch_gemm_t<NORMCOSINE>(a, kpad, dtiles, xaux, qtiles, q_norm, st);
+        case COSINE: return launch_gemm_t<COSINE>(a, kpad, dtiles, xaux, qtiles, q_norm, st);
+        case IP: return launch_gemm_t<IP>(a, kpad, dtiles, xaux, qtiles, q_norm, st);
         default: return cudaErrorInvalidValue;
     }
 }

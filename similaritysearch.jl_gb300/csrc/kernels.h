@@ -147,7 +147,13 @@ cudaError_t launch_stream_scan(const uint8_t *q_tiles, const uint8_t *d_tiles, c
 // Writes `splits` sorted segments of kk keys per query.
 bool gemm_fits(int kk);
 int gemm_ctas_per_sm(int kk);
-cudaError_t launch_gemm_f32(const ScanArgs &a, const float *db, const float *xaux, const float *q,
+// k-major tiles of 128 rows (dim-major, zero-padded to gemm_kpad(dim)).
+int gemm_kpad(int64_t dim);
+size_t gemm_tile_floats(int64_t dim);
+cudaError_t launch_gemm_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, float *out, cudaStream_t st,
+                              int *launches);
+// a.split_len must be a multiple of 128 (tile-aligned splits).
+cudaError_t launch_gemm_f32(const ScanArgs &a, const float *dtiles, const float *xaux, const float *qtiles,
                             const float *q_norm, cudaStream_t st, int *launches);
 
 // ---- helpers (direct.cu) ----
