@@ -53,6 +53,7 @@ K = 32
 N_CENTRES = 1000
 HEADLINE_MODE = "bf16"
 HEADLINE_OVERFETCH = 1.25
+HEADLINE_SCAN_TRAFFIC = 191.58e9 + 0.687e9
 
 METRIC = "queries/s @ recall@10>=0.99 (allknn NormCosine n=1e6 d=96 k=32 excl. self)"
 DATA = ("synthetic: seeded 1000-cluster Gaussian mixture (centres N(0,1), sigma U[0.1,0.5]), "
@@ -338,6 +339,11 @@ def allknn_mode(cx, X, mode, overfetch, steps, warmup):
     avg = main_ms / max(1, main_launches)
     q_per_launch = n * steps / max(1, main_launches)
     roof = roofline_flops(mode, 2.0 * q_per_launch * n * d, avg)
+    if mode == "bf16" and n == 1_000_000 and d == 96 and main_launches == steps:
+        # DRAM bytes (read + write) of one headline scan launch, from one ncu
+        # capture of it (1-pass dram__bytes_read/write.sum metrics)
+        roof["traffic"] = HEADLINE_SCAN_TRAFFIC
+        roof["traffic_note"] = "dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of this launch"
     return {"ms_per_step": ms, "qps": cx.world * n / (ms / 1e3), "launches": launches, "roofline": roof,
             "clocks": clocks, "ids": ids_host}
 

@@ -85,6 +85,14 @@ int ssg_create(int metric, int elem_type, int64_t dim, int64_t n,
 int ssg_create_device(int metric, int elem_type, int64_t dim, int64_t n,
                       const void *dev_db, int64_t ld, int precision_mode, ssg_index **out);
 
+/* Same, from a MMapMatrixDatabase file (src/db/mmapmatrixdatabase.jl:10-27,
+ * 151-175): a 4096-byte header (magic 0x4D4D444231000001, version 1, dim,
+ * element type code, n) followed by the column-major data, which streams
+ * from the mapped file into device memory (no host copy of the whole file).
+ * Element types: Float32, Float64, Float16, Int8, UInt8 (cast to Float32 for
+ * the float metrics, as the CastF32 twins do) and UInt64 (HAMMING). */
+int ssg_create_mmap(int metric, const char *path, int precision_mode, ssg_index **out);
+
 /* k nearest neighbours of `m` queries (host rows of `dim` elements of the
  * index's element type, contiguous) written to host out_ids / out_dists
  * (m rows of k).  Replaces the matrix searchbatch! loop
@@ -200,6 +208,19 @@ int ssg_mlp_grad_check(int64_t d, int64_t hidden, int64_t out_dim, const float *
                        const float *b1, const float *W2, const float *b2, const float *X,
                        int32_t batch, float margin, float *loss, float *gW1, float *gb1,
                        float *gW2, float *gb2);
+
+/* Bit sketches (bitsketch(R, X), src/proj/bitsketches.jl:19-32,56-57,101-104
+ * over transform, src/proj/Projections.jl:137-143): for each of the n rows x
+ * of dev_X (n rows of dim Float32) and each of the outdim projection rows r
+ * of dev_R (outdim rows of dim Float32: the bytes of the Julia (dim, outdim)
+ * map), bit c of the row's sketch is 1 iff dot(r_c, x) >= 0, packed 64 per
+ * UInt64 word (coordinate c in bit c % 64 of word c / 64, unused high bits
+ * 0) into dev_out (n rows of ceil(outdim / 64) words): the C3 sketches the
+ * Hamming scan searches.  The dot products are the sequential FP32 fma
+ * chain.  Device buffers; work on `stream` (cudaStream_t, NULL = default),
+ * the call returns when it is done. */
+int ssg_bitsketch(const void *dev_R, int64_t dim, int64_t outdim, const void *dev_X, int64_t n,
+                  uint64_t *dev_out, void *stream);
 
 /* Exact k-NN that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- programs

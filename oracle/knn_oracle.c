@@ -429,6 +429,25 @@ double oracle_macrorecall(const uint32_t *gold, int64_t kg, const uint32_t *res,
     return s / (double)m;
 }
 
+/* bitsketch(R, X) (src/proj/bitsketches.jl:101-104 via _bitsketch_apply,
+ * :56-57): transform (src/proj/Projections.jl:137-143: coordinate c of row r
+ * is dot32(R column c, x_r)), then packsigns (bitsketches.jl:19-32: bit c of
+ * word c / 64 set iff the coordinate is >= 0, unused high bits 0).  R is
+ * given as outdim rows of indim (the bytes of the Julia (indim, outdim)
+ * matrix); out is n rows of ceil(outdim / 64) words. */
+void oracle_bitsketch(const float *R, int64_t indim, int64_t outdim, const float *X, int64_t n,
+                      uint64_t *out, int lanes)
+{
+    const int64_t words = (outdim + 63) / 64;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t r = 0; r < n; ++r) {
+        uint64_t *o = out + r * words;
+        for (int64_t w = 0; w < words; ++w) o[w] = 0;
+        for (int64_t c = 0; c < outdim; ++c)
+            if (dot32(R + c * indim, X + r * indim, indim, lanes) >= 0.0f) o[c >> 6] |= (uint64_t)1 << (c & 63);
+    }
+}
+
 int oracle_num_threads(void)
 {
 #ifdef _OPENMP

@@ -63,6 +63,8 @@ def lib():
             L.oracle_searchbatch_f64.argtypes = [_int, _p, _i64, _i64, _p, _i64, _i32, _p, _p, _int]
             L.oracle_rerank.argtypes = [_int, _p, _i64, _p, _p, _p, _i32, _int]
             L.oracle_macrorecall.argtypes = [_p, _i64, _p, _i64, _i64, _i64]
+            L.oracle_bitsketch.argtypes = [_p, _i64, _i64, _p, _i64, _p, _int]
+            L.oracle_bitsketch.restype = None
             L.oracle_macrorecall.restype = C.c_double
             L.oracle_num_threads.restype = _int
             _lib = L
@@ -110,6 +112,18 @@ class KnnSorted:
     def items(self):
         s, e = self._sp.value - 1, self._ep.value
         return list(zip(self.ids[s:e].tolist(), self.dists[s:e].tolist()))
+
+
+def bitsketch(R, X, lanes: int = 1) -> np.ndarray:
+    """Sign sketches of the rows of X (n x indim) against the projection R
+    given as outdim rows of indim: n rows of ceil(outdim / 64) UInt64 words
+    (oracle_bitsketch; src/proj/bitsketches.jl:19-32,56-57,101-104)."""
+    R = np.ascontiguousarray(R, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    assert R.shape[1] == X.shape[1]
+    out = np.zeros((X.shape[0], (R.shape[0] + 63) // 64), dtype=np.uint64)
+    lib().oracle_bitsketch(_ptr(R), R.shape[1], R.shape[0], _ptr(X), X.shape[0], _ptr(out), lanes)
+    return out
 
 
 def evaluate(metric, a, b, lanes: int = 1) -> float:

@@ -5,7 +5,8 @@ GPU index (``GPUExhaustiveSearch``) whose work is done by libssgpu.so, the
 sm_103a CUDA library with the C ABI of ``include/ssgpu.h``.
 """
 from . import _native, shard
-from .db import AbstractDatabase, MatrixDatabase, VectorDatabase
+from .proj import bitsketch
+from .db import AbstractDatabase, MatrixDatabase, MMapMatrixDatabase, VectorDatabase, write_mmap_matrix
 from .dist import Dist, PreMetric, evaluate
 from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,
                     allknn, allknn_b, append_items_b, database, distance, distance_evaluations, index_b,
@@ -19,12 +20,12 @@ from .pqueue import IdDist, KnnSorted, knnqueue
 GPUParallelExhaustiveSearch = GPUExhaustiveSearch
 
 __all__ = [
-    "AbstractDatabase", "MatrixDatabase", "VectorDatabase", "Dist", "PreMetric", "evaluate",
+    "AbstractDatabase", "MatrixDatabase", "MMapMatrixDatabase", "VectorDatabase", "write_mmap_matrix", "Dist", "PreMetric", "evaluate",
     "ArgumentError", "GenericContext", "GPUExhaustiveSearch", "GPUParallelExhaustiveSearch",
     "add_distance_evaluations", "allknn", "allknn_b", "append_items_b", "database", "distance",
     "distance_evaluations", "index_b", "push_item_b", "rerank_b", "search", "searchbatch",
     "searchbatch_b", "searchbatches", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
-    "IdDist", "KnnSorted", "knnqueue",
+    "IdDist", "KnnSorted", "knnqueue", "bitsketch",
 ]
 
 

@@ -12,6 +12,10 @@
 #include "kernels.h"
 
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cstdarg>
@@ -1336,6 +1340,63 @@ int ssg_create_device(int metric, int elem_type, int64_t dim, int64_t n, const v
     return create_common(metric, elem_type, dim, n, dev_db, ld, precision_mode, out, true);
 }
 
+int ssg_create_mmap(int metric, const char *path, int precision_mode, ssg_index **out) {
+    if (!path || !out) return fail(nullptr, SSG_EINVAL, "NULL path or output");
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) return fail(nullptr, SSG_EINVAL, "cannot open '%s'", path);
+    struct stat st;
+    unsigned char hdr[32];
+    if (fstat(fd, &st) != 0 || st.st_size < 4096 || pread(fd, hdr, sizeof hdr, 0) != ssize_t(sizeof hdr)) {
+        close(fd);
+        return fail(nullptr, SSG_EINVAL, "'%s' is not a matrix database file (short header)", path);
+    }
+    // header (src/db/mmapmatrixdatabase.jl:10-27): magic u64 @0, version i32 @8,
+    // dim i64 @12, element type code i32 @20, n i64 @24, data from byte 4096
+    uint64_t magic;
+    int32_t version, code;
+    int64_t dim, n;
+    memcpy(&magic, hdr + 0, 8);
+    memcpy(&version, hdr + 8, 4);
+    memcpy(&dim, hdr + 12, 8);
+    memcpy(&code, hdr + 20, 4);
+    memcpy(&n, hdr + 24, 8);
+    int elem = -1;
+    size_t es = 0;
+    switch (code) {  // Float16 1, Float32 2, Float64 3, Int8 4, UInt8 5, UInt64 11
+        case 1: elem = SSG_ELEM_F16; es = 2; break;
+        case 2: elem = SSG_ELEM_F32; es = 4; break;
+        case 3: elem = SSG_ELEM_F64; es = 8; break;
+        case 4: elem = SSG_ELEM_I8; es = 1; break;
+        case 5: elem = SSG_ELEM_U8; es = 1; break;
+        case 11: elem = SSG_ELEM_U64; es = 8; break;
+        default: break;
+    }
+    int rc = SSG_OK;
+    if (magic != 0x4D4D444231000001ull || version != 1) {
+        rc = fail(nullptr, SSG_EINVAL, "'%s' is not a matrix database file (magic / version)", path);
+    } else if (elem < 0) {
+        rc = fail(nullptr, SSG_EUNSUPPORTED, "element type code %d is not supported", code);
+    } else if (dim <= 0 || n < 0 || (int64_t(st.st_size) - 4096) / int64_t(es) / dim < n) {
+        rc = fail(nullptr, SSG_EINVAL, "corrupt matrix database file: dim %lld, n %lld, %lld bytes", (long long)dim,
+                  (long long)n, (long long)st.st_size);
+    }
+    if (rc) {
+        close(fd);
+        return rc;
+    }
+    // map the file and upload from the mapping: pages stream from the file
+    // (page cache) through the upload, no copy of the whole file in host memory
+    const size_t bytes = 4096 + size_t(n) * size_t(dim) * es;
+    void *map = n > 0 ? mmap(nullptr, bytes, PROT_READ, MAP_SHARED, fd, 0) : nullptr;
+    close(fd);
+    if (n > 0 && map == MAP_FAILED) return fail(nullptr, SSG_ENOMEM, "cannot map '%s'", path);
+    if (map) madvise(map, bytes, MADV_SEQUENTIAL);
+    rc = create_common(metric, elem, dim, n, map ? static_cast<const char *>(map) + 4096 : nullptr, dim,
+                       precision_mode, out, false);
+    if (map) munmap(map, bytes);
+    return rc;
+}
+
 int ssg_search(ssg_index *idx, const void *host_q, int64_t dim, int64_t m, int32_t k, uint32_t *out_ids,
                float *out_dists, int32_t flags) {
     return search_common(idx, host_q, dim, m, k, out_ids, out_dists, flags, false);
@@ -1551,6 +1612,39 @@ int ssg_last_error(ssg_index *idx, char *buf, int64_t len) {
         buf[c] = '\0';
     }
     return full;
+}
+
+int ssg_bitsketch(const void *dev_R, int64_t dim, int64_t outdim, const void *dev_X, int64_t n, uint64_t *dev_out,
+                  void *stream) {
+    if (dim <= 0 || outdim <= 0 || n < 0 || outdim > (int64_t(1) << 24) || dim > (int64_t(1) << 24))
+        return fail(nullptr, SSG_EINVAL, "bitsketch needs dim > 0 and 0 < outdim <= 2^24");
+    if (n == 0) return SSG_OK;
+    if (!dev_R || !dev_X || !dev_out) return fail(nullptr, SSG_EINVAL, "NULL buffer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t tf = ssg::gemm_tile_floats(dim);
+    const int64_t xt = (n + 127) / 128, rt = (outdim + 127) / 128;
+    void *xtiles = nullptr, *rtiles = nullptr;
+    cudaError_t e = cudaMallocAsync(&xtiles, size_t(xt) * tf * 4, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&rtiles, size_t(rt) * tf * 4, st);
+    int launches = 0;
+    if (e == cudaSuccess)
+        e = ssg::launch_gemm_tiles(static_cast<const float *>(dev_X), n, dim, xt, static_cast<float *>(xtiles), st,
+                                   &launches);
+    if (e == cudaSuccess)
+        e = ssg::launch_gemm_tiles(static_cast<const float *>(dev_R), outdim, dim, rt, static_cast<float *>(rtiles),
+                                   st, &launches);
+    if (e == cudaSuccess)
+        e = ssg::launch_bitsketch(static_cast<const float *>(xtiles), static_cast<const float *>(rtiles), dim, n,
+                                  outdim, dev_out, st, &launches);
+    if (xtiles) cudaFreeAsync(xtiles, st);
+    if (rtiles) cudaFreeAsync(rtiles, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, e == cudaErrorMemoryAllocation ? SSG_ENOMEM : SSG_ECUDA, "bitsketch: %s",
+                    cudaGetErrorString(e));
+    }
+    return SSG_OK;
 }
 
 int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t epochs, int32_t hidden,

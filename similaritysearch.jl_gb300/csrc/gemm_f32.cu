@@ -100,6 +100,99 @@ __global__ void gemm_tile_kernel(const float *__restrict__ x, int64_t rows, int 
     }
 }
 
+// acc[i][j] = sum_k A[row_i][k] * B[col_j][k] over the k-major tiles `qtile`
+// (rows ty*4+i and 64+ty*4+i) and `dtile` (columns tx*4+j and 64+tx*4+j),
+// one fmaf per k in increasing k: the sequential dot-product chain.  Uses
+// the operand ring sA / sB; the caller has synchronised before it is reused.
+__device__ __forceinline__ void tile_products(float (&acc)[8][8], float *sA, float *sB, const float *qtile,
+                                              const float *dtile, int kpad) {
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int nslices = kpad / BK;
+    // prologue: slices 0 .. STAGES-2 in flight (one commit group each, maybe empty)
+#pragma unroll
+    for (int p = 0; p < STAGES - 1; ++p) {
+        if (p < nslices) {
+            load_slice_async(sA + p * BK * LDA, qtile, p * BK);
+            load_slice_async(sB + p * BK * LDA, dtile, p * BK);
+        }
+        cp_async_commit();
+    }
+    for (int sl = 0; sl < nslices; ++sl) {
+        cp_async_wait_ahead();
+        __syncthreads();  // slice sl visible; the buffer of slice sl-1 is free
+        if (sl + STAGES - 1 < nslices) {
+            const int nb = (sl + STAGES - 1) % STAGES;
+            load_slice_async(sA + nb * BK * LDA, qtile, (sl + STAGES - 1) * BK);
+            load_slice_async(sB + nb * BK * LDA, dtile, (sl + STAGES - 1) * BK);
+        }
+        cp_async_commit();
+        const int buf = sl % STAGES;
+        const float *cA = sA + buf * BK * LDA;
+        const float *cB = sB + buf * BK * LDA;
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(cA + kk * LDA + ty * 4);
+            const float4 a1 = *reinterpret_cast<const float4 *>(cA + kk * LDA + 64 + ty * 4);
+            const float4 b0 = *reinterpret_cast<const float4 *>(cB + kk * LDA + tx * 4);
+            const float4 b1 = *reinterpret_cast<const float4 *>(cB + kk * LDA + 64 + tx * 4);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(bv[j], av[i], acc[i][j]);
+        }
+    }
+    cp_async_wait_all();
+}
+
+// Bit sketches: bit c of row r's sketch is set iff sum_k X[r][k] * R[c][k] >= 0
+// (sequential fma chain), packed 64 coordinates per UInt64 word, coordinate c
+// in bit c % 64 of word c / 64 (bitsketch / packsigns, src/proj/bitsketches.jl:
+// 19-32,56-57,101-104; transform!, src/proj/Projections.jl:137-143).  A CTA
+// computes a 128-row x 128-coordinate tile and writes 128 x 2 words.
+__global__ void __launch_bounds__(THREADS, 2)
+bitsketch_kernel(const float *__restrict__ xtiles, const float *__restrict__ rtiles, int kpad, int64_t n, int outdim,
+                 int words, uint64_t *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *sA = reinterpret_cast<float *>(smem);
+    float *sB = sA + STAGES * BK * LDA;
+    uint8_t *sbits = smem;  // [128][128] sign bytes, aliases the operands after the products
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    tile_products(acc, sA, sB, xtiles + size_t(blockIdx.x) * kpad * BM, rtiles + size_t(blockIdx.y) * kpad * BN,
+                  kpad);
+    __syncthreads();  // operands no longer read
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = (i < 4 ? 0 : 64) + ty * 4 + (i & 3);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = (j < 4 ? 0 : 64) + tx * 4 + (j & 3);
+            sbits[r * BN + c] = acc[i][j] >= 0.0f ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    // thread -> (row, 64-coordinate half): one output word
+    const int r = tid >> 1, h = tid & 1;
+    const int64_t row = int64_t(blockIdx.x) * BM + r;
+    const int word = blockIdx.y * 2 + h;
+    if (row >= n || word >= words) return;
+    uint64_t w = 0;
+    const uint8_t *src = sbits + r * BN + h * 64;
+    for (int b = 0; b < 64; ++b) {
+        const int c = word * 64 + b;
+        if (c < outdim && src[b]) w |= uint64_t(1) << b;
+    }
+    out[size_t(row) * words + word] = w;
+}
+
 template <int METRIC>
 __global__ void __launch_bounds__(THREADS, 2)
 gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const float *__restrict__ xaux,
@@ -132,44 +225,7 @@ gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const fl
             for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 
         __syncthreads();  // the previous tile's epilogue is done with shared memory
-        const int nslices = kpad / BK;
-        const float *dtile = dtiles + size_t(j0 / BN) * kpad * BN;
-        // prologue: slices 0 .. STAGES-2 in flight (one commit group each, maybe empty)
-#pragma unroll
-        for (int p = 0; p < STAGES - 1; ++p) {
-            if (p < nslices) {
-                load_slice_async(sA + p * BK * LDA, qtile, p * BK);
-                load_slice_async(sB + p * BK * LDA, dtile, p * BK);
-            }
-            cp_async_commit();
-        }
-        for (int sl = 0; sl < nslices; ++sl) {
-            cp_async_wait_ahead();
-            __syncthreads();  // slice sl visible; the buffer of slice sl-1 is free
-            if (sl + STAGES - 1 < nslices) {
-                const int nb = (sl + STAGES - 1) % STAGES;
-                load_slice_async(sA + nb * BK * LDA, qtile, (sl + STAGES - 1) * BK);
-                load_slice_async(sB + nb * BK * LDA, dtile, (sl + STAGES - 1) * BK);
-            }
-            cp_async_commit();
-            const int buf = sl % STAGES;
-            const float *cA = sA + buf * BK * LDA;
-            const float *cB = sB + buf * BK * LDA;
-#pragma unroll
-            for (int kk = 0; kk < BK; ++kk) {
-                const float4 a0 = *reinterpret_cast<const float4 *>(cA + kk * LDA + ty * 4);
-                const float4 a1 = *reinterpret_cast<const float4 *>(cA + kk * LDA + 64 + ty * 4);
-                const float4 b0 = *reinterpret_cast<const float4 *>(cB + kk * LDA + tx * 4);
-                const float4 b1 = *reinterpret_cast<const float4 *>(cB + kk * LDA + 64 + tx * 4);
-                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-                const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(bv[j], av[i], acc[i][j]);
-            }
-        }
-        cp_async_wait_all();
+        tile_products(acc, sA, sB, qtile, dtiles + size_t(j0 / BN) * kpad * BN, kpad);
         // epilogue, in two halves of 64 query rows staged through the operands
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -257,6 +313,20 @@ cudaError_t launch_gemm_tiles(const float *x, int64_t rows, int64_t dim, int64_t
     dim3 grid(unsigned(tiles * BM / 32), unsigned((kpad + 31) / 32));
     if (launches) *launches += 1;
     gemm_tile_kernel<<<grid, dim3(32, 8), 0, st>>>(x, rows, int(dim), kpad, tiles, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bitsketch(const float *xtiles, const float *rtiles, int64_t dim, int64_t n, int64_t outdim,
+                             uint64_t *out, cudaStream_t st, int *launches) {
+    if (n <= 0 || outdim <= 0) return cudaSuccess;
+    const int kpad = gemm_kpad(dim);
+    const int words = int((outdim + 63) / 64);
+    const size_t smem = GemmSmem::operands() > size_t(BM) * BN ? GemmSmem::operands() : size_t(BM) * BN;
+    cudaError_t e = cudaFuncSetAttribute(bitsketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((n + BM - 1) / BM), unsigned((outdim + BN - 1) / BN));
+    if (launches) *launches += 1;
+    bitsketch_kernel<<<grid, THREADS, smem, st>>>(xtiles, rtiles, kpad, n, int(outdim), words, out);
     return cudaGetLastError();
 }
 

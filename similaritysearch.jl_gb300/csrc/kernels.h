@@ -152,6 +152,10 @@ int gemm_kpad(int64_t dim);
 size_t gemm_tile_floats(int64_t dim);
 cudaError_t launch_gemm_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, float *out, cudaStream_t st,
                               int *launches);
+// Sign bit sketches of n rows against outdim projection rows, from k-major
+// tiles of both (out: n rows of ceil(outdim / 64) words).
+cudaError_t launch_bitsketch(const float *xtiles, const float *rtiles, int64_t dim, int64_t n, int64_t outdim,
+                             uint64_t *out, cudaStream_t st, int *launches);
 // a.split_len must be a multiple of 128 (tile-aligned splits).
 cudaError_t launch_gemm_f32(const ScanArgs &a, const float *dtiles, const float *xaux, const float *qtiles,
                             const float *q_norm, cudaStream_t st, int *launches);

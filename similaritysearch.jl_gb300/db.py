@@ -99,6 +99,60 @@ class VectorDatabase(AbstractDatabase):
             self.push_item(v)
 
 
+# MMapMatrixDatabase files (src/db/mmapmatrixdatabase.jl:10-27): a 4096-byte
+# header -- magic UInt64 @0, version Int32 @8, dim Int64 @12, element type
+# code Int32 @20, length n Int64 @24 -- then the column-major (dim, capacity)
+# data, little-endian.
+MMAP_MAGIC = 0x4D4D444231000001
+MMAP_HEADER = 4096
+_MMAP_CODES = {np.dtype(np.float16): 1, np.dtype(np.float32): 2, np.dtype(np.float64): 3, np.dtype(np.int8): 4,
+               np.dtype(np.uint8): 5, np.dtype(np.int16): 6, np.dtype(np.uint16): 7, np.dtype(np.int32): 8,
+               np.dtype(np.uint32): 9, np.dtype(np.int64): 10, np.dtype(np.uint64): 11}
+_MMAP_TYPES = {v: k for k, v in _MMAP_CODES.items()}
+
+
+def write_mmap_matrix(path, X, capacity: int | None = None):
+    """Writes the ``(dim, n)`` matrix X as a MMapMatrixDatabase file (spare
+    capacity columns are zero, as the reference preallocates)."""
+    X = np.asarray(X)
+    dim, n = X.shape
+    cap = max(n, capacity or n)
+    hdr = bytearray(MMAP_HEADER)
+    hdr[0:8] = np.uint64(MMAP_MAGIC).tobytes()
+    hdr[8:12] = np.int32(1).tobytes()
+    hdr[12:20] = np.int64(dim).tobytes()
+    hdr[20:24] = np.int32(_MMAP_CODES[X.dtype]).tobytes()
+    hdr[24:32] = np.int64(n).tobytes()
+    with open(path, "wb") as f:
+        f.write(bytes(hdr))
+        f.write(np.asfortranarray(X).tobytes(order="F"))
+        f.write(bytes((cap - n) * dim * X.dtype.itemsize))
+
+
+class MMapMatrixDatabase(MatrixDatabase):
+    """Read-only view of a MMapMatrixDatabase file (the reference's reopen
+    constructor, mmapmatrixdatabase.jl:151-175).  GPUExhaustiveSearch builds
+    its device copy straight from the file (``ssg_create_mmap``)."""
+
+    def __init__(self, path):
+        self.path = str(path)
+        with open(self.path, "rb") as f:
+            hdr = f.read(32)
+        if len(hdr) < 32 or int(np.frombuffer(hdr[0:8], "<u8")[0]) != MMAP_MAGIC:
+            raise ValueError(f"{path} is not a MMapMatrixDatabase file (bad magic)")
+        if int(np.frombuffer(hdr[8:12], "<i4")[0]) != 1:
+            raise ValueError("unsupported MMapMatrixDatabase version")
+        dim = int(np.frombuffer(hdr[12:20], "<i8")[0])
+        code = int(np.frombuffer(hdr[20:24], "<i4")[0])
+        n = int(np.frombuffer(hdr[24:32], "<i8")[0])
+        if code not in _MMAP_TYPES:
+            raise ValueError(f"unknown element type code {code}")
+        dt = _MMAP_TYPES[code]
+        mat = np.memmap(self.path, dtype=dt, mode="r", offset=MMAP_HEADER, shape=(dim, n), order="F") if n \
+            else np.zeros((dim, 0), dtype=dt)
+        super().__init__(mat)
+
+
 def as_database(x) -> AbstractDatabase:
     if isinstance(x, AbstractDatabase):
         return x

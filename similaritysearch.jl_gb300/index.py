@@ -22,7 +22,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
-from .db import AbstractDatabase, MatrixDatabase, VectorDatabase, as_database
+from .db import AbstractDatabase, MatrixDatabase, MMapMatrixDatabase, VectorDatabase, as_database
 from .dist import PreMetric
 from .log import LOG, InformativeLog
 from .pqueue import AbstractKnnQueue, KnnSorted
@@ -95,8 +95,12 @@ class GPUExhaustiveSearch:
         self.dim = rows.shape[1]
         h = C.c_void_p()
         lib = N.lib()
-        N.check(lib.ssg_create(dist.code, self._elem, self.dim, rows.shape[0], rows.ctypes.data_as(C.c_void_p),
-                               self.dim, _PREC[precision], C.byref(h)))
+        if isinstance(self.db, MMapMatrixDatabase):
+            # straight from the file into device memory
+            N.check(lib.ssg_create_mmap(dist.code, self.db.path.encode(), _PREC[precision], C.byref(h)))
+        else:
+            N.check(lib.ssg_create(dist.code, self._elem, self.dim, rows.shape[0], rows.ctypes.data_as(C.c_void_p),
+                                   self.dim, _PREC[precision], C.byref(h)))
         self._h = h
         for k, v in params.items():
             self.set_param(k, v)

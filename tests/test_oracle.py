@@ -181,3 +181,22 @@ def test_f64_gold_matches_f32_on_separated_data():
     gi, _ = O.searchbatch_f64("sql2", db, Q, 10)
     fi, _ = O.searchbatch("sql2", db, Q, 10)
     assert O.macrorecall(gi, fi) == 1.0
+
+
+def test_oracle_bitsketch_semantics():
+    # packsigns (src/proj/bitsketches.jl:19-32): >= 0 -> bit 1 (zero included),
+    # coordinate c in bit c % 64 of word c / 64, unused high bits 0;
+    # cld(outdim, 64) words per sketch (test/testprojections.jl:67-75)
+    R = np.zeros((70, 4), dtype=np.float32)        # outdim = 70 projection rows of indim = 4
+    R[1] = [1, 0, 0, 0]
+    R[2] = [-1, 0, 0, 0]
+    R[65] = [0, 0, 0, -2]
+    X = np.array([[1, 2, 3, 4], [-1, 0, 0, 1]], dtype=np.float32)
+    B = O.bitsketch(R, X)
+    assert B.shape == (2, 2) and B.dtype == np.uint64
+    for r in range(2):
+        bits = [(int(B[r, c // 64]) >> (c % 64)) & 1 for c in range(70)]
+        for c in range(70):
+            assert bits[c] == (1 if float(np.dot(R[c], X[r])) >= 0 else 0)
+        assert int(B[r, 1]) >> 6 == 0               # coordinates 70..127 do not exist
+    assert (int(B[0, 0]) >> 2) & 1 == 0 and (int(B[1, 0]) >> 2) & 1 == 1
