@@ -60,6 +60,16 @@ __host__ __device__ constexpr int col_splits() { return QT == 1 ? 2 : 1; }
 template <int QT>
 __host__ __device__ constexpr int tc_threads() { return 64 + TILE * QT * col_splits<QT>(); }
 
+// TMEM accumulators per query tile: 4 x 128 columns with one query tile per
+// CTA (all 512 columns), so the MMAs run up to three tiles ahead of the
+// epilogue; 2 with two query tiles, and for the threshold filter, whose
+// CTAs may share an SM.  A CTA holding all 512 columns is given enough
+// shared memory to be alone on its SM (tcgen05.alloc would otherwise wait
+// for the other CTA to finish).
+template <int QT, bool FILTER>
+__host__ __device__ constexpr int acc_buffers() { return (QT == 1 && !FILTER) ? 4 : 2; }
+constexpr size_t kAloneSmem = 120 * 1024;
+
 int metric_class(int metric) {
     if (metric == SQL2 || metric == L2) return MC_SQ;
     if (metric == COSINE) return MC_COS;
@@ -156,6 +166,7 @@ __device__ __forceinline__ int tc_live_warps(const TcArgs &a) {
 template <int QT, int STAGES, int MC, bool FILTER>
 __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) {
     constexpr int CS = col_splits<QT>();
+    constexpr int NACC = acc_buffers<QT, FILTER>();
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -169,11 +180,11 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
     uint64_t *full = bars + 1;
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
-    uint64_t *acc_empty = acc_full + 2;
-    uint64_t *mma_done = acc_empty + 2;
+    uint64_t *acc_empty = acc_full + NACC;
+    uint64_t *mma_done = acc_empty + NACC;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
 
-    constexpr int NCOLS = QT * 2 * TILE;  // 256 or 512
+    constexpr int NCOLS = QT * NACC * TILE;  // all 512 TMEM columns
     const int warp = threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
 
@@ -183,7 +194,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NACC; ++b) {
             tc::mbar_init(&acc_full[b], 1);
             tc::mbar_init(&acc_empty[b], tc_live_warps<QT, CS>(a));
         }
@@ -232,14 +243,14 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             int issued = 0;
             for (int t = 0; ok && t < T_tiles; ++t) {
                 const int s = t % STAGES;
-                const int b = t & 1;
+                const int b = t % NACC;
                 if (!tc::mbar_wait(&full[s], (t / STAGES) & 1, a.err, 4)) break;
-                if (!tc::mbar_wait(&acc_empty[b], ((t >> 1) & 1) ^ 1, a.err, 5)) break;
+                if (!tc::mbar_wait(&acc_empty[b], ((t / NACC) & 1) ^ 1, a.err, 5)) break;
                 tc::tc_fence_after();
                 const uint32_t b_addr = b_addr0 + uint32_t(s * tile_bytes);
 #pragma unroll
                 for (int q = 0; q < QT; ++q) {
-                    const uint32_t d_tmem = tmem_base + uint32_t((q * 2 + b) * TILE);
+                    const uint32_t d_tmem = tmem_base + uint32_t((q * NACC + b) * TILE);
                     for (int kk = 0; kk < ksteps; ++kk) {
                         const uint32_t kbyte = uint32_t(kk) * 32u;
                         const uint32_t blk_off = (kbyte / SW) * (TILE * SW) + (kbyte % SW);
@@ -278,9 +289,9 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         float topd = qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
         int nbuf = 0;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
-            const int b = t & 1;
+            const int b = t % NACC;
             int ok = 1;
-            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 7) ? 1 : 0;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t / NACC) & 1, a.err, 7) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
@@ -290,7 +301,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             uint32_t r[CHUNKS][32];
             __syncwarp();
             const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) +
-                                   uint32_t((q * 2 + b) * TILE + cs * (TILE / CS));
+                                   uint32_t((q * NACC + b) * TILE + cs * (TILE / CS));
 #pragma unroll
             for (int c = 0; c < CHUNKS; ++c) tc::tmem_ld_32x32b_x32_async(tbase + uint32_t(c * 32), r[c]);
             tc::tmem_wait_ld();
@@ -371,7 +382,8 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
 
 template <int QT, int STAGES, int MC, bool FILTER>
 cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
-    const size_t smem = TcSmem<QT, STAGES>::total(a.kp, a.kk);
+    size_t smem = TcSmem<QT, STAGES>::total(a.kp, a.kk);
+    if (acc_buffers<QT, FILTER>() * QT * TILE == 512 && smem < kAloneSmem) smem = kAloneSmem;
     auto kern = tc_scan_kernel<QT, STAGES, MC, FILTER>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;

@@ -40,6 +40,9 @@ constexpr int KBLOCK_BYTES = TILE * SWB;      // 16 KB per operand per K-block
 constexpr int kBufCap = 12;
 constexpr int kDrainTrigger = 4;
 constexpr int kDrainEvery = 8;
+// TMEM accumulators (128 columns each): all 512 columns, so the MMAs run up
+// to three tiles ahead of the epilogue
+constexpr int NACC = 4;
 
 template <int CS>
 __host__ __device__ constexpr int st_threads() { return 64 + TILE * CS; }
@@ -242,11 +245,11 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
     uint64_t *full = bars;
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
-    uint64_t *acc_empty = acc_full + 2;
-    uint64_t *mma_done = acc_empty + 2;
+    uint64_t *acc_empty = acc_full + NACC;
+    uint64_t *mma_done = acc_empty + NACC;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
 
-    constexpr int NCOLS = 2 * TILE;
+    constexpr int NCOLS = NACC * TILE;  // all 512 TMEM columns
     const int warp = threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
 
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NACC; ++b) {
             tc::mbar_init(&acc_full[b], 1);
             tc::mbar_init(&acc_empty[b], stream_live_warps<CS>(a));
         }
@@ -303,8 +306,8 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
             int it = 0;
             bool ok = true;
             for (int t = 0; ok && t < T_tiles; ++t) {
-                const int b = t & 1;
-                if (!tc::mbar_wait(&acc_empty[b], ((t >> 1) & 1) ^ 1, a.err, 13)) break;
+                const int b = t % NACC;
+                if (!tc::mbar_wait(&acc_empty[b], ((t / NACC) & 1) ^ 1, a.err, 13)) break;
                 tc::tc_fence_after();
                 const uint32_t d_tmem = tmem_base + uint32_t(b * TILE);
                 for (int kb = 0; kb < KB; ++kb, ++it) {
@@ -353,9 +356,9 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
         sb.init(shared ? a.gbound + size_t(query) * kBoundWords : nullptr, a.splits * CS, a.kk);
         int nbuf = 0;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
-            const int b = t & 1;
+            const int b = t % NACC;
             int ok = 1;
-            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t >> 1) & 1, a.err, 16) ? 1 : 0;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (t / NACC) & 1, a.err, 16) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
