@@ -118,7 +118,7 @@ int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k,
  * candidate list at least as long).  Batches with m[b] == 0 are skipped.
  * Replaces per-request searchbatch! calls on a request stream.  With the
  * reduced-precision scans the device work of a call is replayed from a CUDA
- * graph when its shape (queries rounded up to 128, largest k) repeats
+ * graph when its shape (queries rounded up to 32, largest k) repeats
  * ("graphs" param, default 1; "graph_replays", "last_graph" readable). */
 int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, const int64_t *m,
                        const int32_t *k, uint32_t *const *dev_ids, float *const *dev_dists);

@@ -600,6 +600,7 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
             f.n_total = idx->n;
             f.flags = flags + c0;
             f.flag_count = flag_count;
+            f.n_rows = idx->n;
             SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
                                                static_cast<const float *>(idx->db_norm.p), idx->dim, qc,
                                                nullptr, idx->stream, &idx->last_launches),
@@ -752,6 +753,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
         const size_t qrow_bytes = size_t(idx->dim) * 4;
+        f.n_rows = idx->n;
         SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
                                            static_cast<const float *>(idx->db_norm.p), idx->dim,
                                            reinterpret_cast<const float *>(static_cast<const char *>(dq) +
@@ -896,6 +898,7 @@ int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t 
         f.self_base = c0;
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
+        f.n_rows = idx->n;
         SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
                                            static_cast<const float *>(idx->db_norm.p), idx->dim,
                                            static_cast<const float *>(dq) + size_t(c0) * idx->dim,
@@ -990,6 +993,7 @@ int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
         f.self_base = c0;
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
+        f.n_rows = idx->n;
         SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
                                            static_cast<const float *>(idx->db_norm.p), idx->dim,
                                            static_cast<const float *>(dq) + size_t(c0) * idx->dim,
@@ -1188,7 +1192,7 @@ int search_graph(ssg_index *idx, const void *q, int64_t m, int32_t k, uint32_t *
             if (rc == SSG_OK && e == cudaSuccess && graph) e = cudaGraphInstantiate(&exec, graph, 0);
             if (graph) cudaGraphDestroy(graph);
             if (rc == SSG_OK && e == cudaSuccess && exec && graph_key(idx, m, k) == key) {
-                if (idx->graphs.size() >= 32) clear_graphs(idx);
+                if (idx->graphs.size() >= 512) clear_graphs(idx);
                 idx->graphs[key] = ssg_index::GraphEntry{exec, idx->last_launches - launches0};
                 it = idx->graphs.find(key);
                 captured = true;
@@ -1426,10 +1430,11 @@ int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, con
     if (idx->n == 0) return fail(idx, SSG_EINVAL, "the index is empty");
     // pack the batches' queries (one copy each), one search with the largest
     // k, then each batch's first k columns back to its own output.  Graph
-    // replays need a fixed shape: the packed count is rounded up to whole
-    // 128-query tiles of zero rows.
+    // replays need a fixed shape: the packed count is rounded up to a
+    // multiple of 32 zero rows (the granularity of the small-batch heaps, so
+    // a small window keeps the small-batch kernel configuration).
     const bool graph = idx->elem == SSG_ELEM_F32 && graph_capturable(idx, kmax);
-    const int64_t mrun = graph ? (mt + 127) / 128 * 128 : mt;
+    const int64_t mrun = graph ? (mt + 31) / 32 * 32 : mt;
     const size_t row_bytes = size_t(idx->dim) * elem_size(idx->elem);
     SSG_CK(idx->pack_q.ensure(size_t(mrun) * row_bytes), "allocating packed queries");
     SSG_CK(idx->pack_out.ensure(size_t(mrun) * kmax * 8), "allocating packed results");

@@ -63,6 +63,9 @@ struct FinalizeArgs {
     int64_t n_total = 0;           // database rows
     int *flags = nullptr;
     int *flag_count = nullptr;
+    // rows of the database the keys index: a key with a larger id is treated
+    // as empty instead of being read (the rerank kernels set it always)
+    int64_t n_rows = 0;
 };
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t st, int *launches);
 

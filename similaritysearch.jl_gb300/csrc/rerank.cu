@@ -98,7 +98,7 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         uint64_t key = KEY_EMPTY;
         if (i < f.kk) {
             const uint64_t ak = s1[i];
-            if (ak != KEY_EMPTY) {
+            if (ak != KEY_EMPTY && int64_t(key_id0(ak)) < f.n_rows) {
                 const uint32_t id0 = key_id0(ak);
                 const float d = exact_pair<METRIC>(db, int64_t(id0), dim, q, j, db_norm, q_norm);
                 key = make_key(d, id0);
