@@ -209,6 +209,21 @@ int ssg_mlp_grad_check(int64_t d, int64_t hidden, int64_t out_dim, const float *
                        int32_t batch, float margin, float *loss, float *gW1, float *gb1,
                        float *gW2, float *gb2);
 
+/* The k closest pairs (i, j) between the indexed objects (i) and the m
+ * objects of host_B (j; rows of dim elements of the index's type), or among
+ * the indexed objects themselves when host_B is NULL (m is then ignored):
+ * bichromatic_kclosestpairs / closestpairs / closestpair
+ * (src/bichromatic/bichromaticclosestpairs.jl, closestpairs.jl,
+ * closestpair.jl).  Each object of B takes its min_k (>= k) nearest indexed
+ * objects -- itself excluded when samedata != 0 (always with host_B NULL),
+ * i.e. when object j of B is indexed object j -- and the k smallest
+ * candidates overall are returned sorted by (distance, j, rank within j),
+ * 1-based ids; *count receives how many exist (< k when there are fewer
+ * pairs; the rest of the outputs are 0 / +Inf).  Outputs are host arrays of
+ * k entries. */
+int ssg_closestpairs(ssg_index *idx, const void *host_B, int64_t m, int32_t k, int32_t min_k,
+                     int32_t samedata, int32_t *out_i, int32_t *out_j, float *out_d, int64_t *count);
+
 /* Bit sketches (bitsketch(R, X), src/proj/bitsketches.jl:19-32,56-57,101-104
  * over transform, src/proj/Projections.jl:137-143): for each of the n rows x
  * of dev_X (n rows of dim Float32) and each of the outdim projection rows r

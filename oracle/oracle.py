@@ -226,3 +226,31 @@ def macrorecall(gold, res, k: int | None = None) -> float:
 
 def num_threads() -> int:
     return int(lib().oracle_num_threads())
+
+
+def closestpairs(metric, A, B, k: int, min_k: int, samedata: bool, lanes: int = 1):
+    """The k closest pairs (i in A, j in B, dist), 1-based, restating
+    bichromatic_kclosestpairs (src/bichromatic/bichromaticclosestpairs.jl):
+    each object j of B is searched for its min_k nearest objects of A
+    (KnnSorted order; with samedata the object itself is excluded, as
+    bichromatic_search! does), its candidates are offered in ascending order
+    to a bounded top-k (insert_topk!), and the buffers are merged.  Ties are
+    ordered by (distance, j, rank), the order the GPU's merge produces; the
+    reference's order among equal distances depends on its batching."""
+    A = np.ascontiguousarray(A)
+    B = np.ascontiguousarray(B)
+    take = min_k + (1 if samedata else 0)
+    take = min(take, A.shape[0])
+    ids, dists = searchbatch(metric, A, B, take, lanes=lanes)
+    cand = []
+    for j in range(B.shape[0]):
+        row = [(float(dists[j, t]), int(ids[j, t])) for t in range(take) if ids[j, t] != 0]
+        if samedata:
+            if any(i == j + 1 for _, i in row):
+                row = [p for p in row if p[1] != j + 1]
+            else:
+                row = row[:-1]
+        for r, (d, i) in enumerate(row[:min_k]):
+            cand.append((d, j + 1, r, i))
+    cand.sort()
+    return [(i, j, d) for d, j, r, i in cand[:k]]

@@ -10,7 +10,8 @@ from .db import AbstractDatabase, MatrixDatabase, MMapMatrixDatabase, VectorData
 from .dist import Dist, PreMetric, evaluate
 from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,
                     allknn, allknn_b, append_items_b, database, distance, distance_evaluations, index_b,
-                    push_item_b, rerank_b, search, searchbatch, searchbatch_b, searchbatches)
+                    push_item_b, rerank_b, search, searchbatch, searchbatch_b, searchbatches,
+                    bichromatic_closestpair, bichromatic_kclosestpairs, closestpair, closestpairs)
 from .log import LOG, InformativeLog, LogList, RecorderLog
 from .perf import macrorecall, recallscore
 from .pqueue import IdDist, KnnSorted, knnqueue
@@ -24,7 +25,8 @@ __all__ = [
     "ArgumentError", "GenericContext", "GPUExhaustiveSearch", "GPUParallelExhaustiveSearch",
     "add_distance_evaluations", "allknn", "allknn_b", "append_items_b", "database", "distance",
     "distance_evaluations", "index_b", "push_item_b", "rerank_b", "search", "searchbatch",
-    "searchbatch_b", "searchbatches", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
+    "searchbatch_b", "searchbatches", "bichromatic_closestpair", "bichromatic_kclosestpairs", "closestpair",
+    "closestpairs", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
     "IdDist", "KnnSorted", "knnqueue", "bitsketch",
 ]
 

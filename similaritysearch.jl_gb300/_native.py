@@ -44,6 +44,7 @@ SIGNATURES = {
     "ssg_last_error": ([_p, C.c_char_p, _i64], _int),
     "ssg_destroy": ([_p], None),
     "ssg_knn_noalloc": ([_int, _p, _i64, _i64, _p, _i64, _i32, _p, _p, _p], _int),
+    "ssg_closestpairs": ([_p, _p, _i64, _i32, _i32, _i32, _p, _p, _p, C.POINTER(_i64)], _int),
     "ssg_bitsketch": ([_p, _i64, _i64, _p, _i64, _p, _p], _int),
     "ssg_search_batches": ([_p, _i32, _p, _p, _p, _p, _p], _int),
     "ssg_train_mlp": ([_p, _i64, _i64, _i32, _i32, _i32, _i32, _dbl, C.c_uint64], _int),

@@ -1619,6 +1619,74 @@ int ssg_last_error(ssg_index *idx, char *buf, int64_t len) {
     return full;
 }
 
+int ssg_closestpairs(ssg_index *idx, const void *host_B, int64_t m, int32_t k, int32_t min_k, int32_t samedata,
+                     int32_t *out_i, int32_t *out_j, float *out_d, int64_t *count) {
+    if (!idx) return fail(nullptr, SSG_EINVAL, "index is NULL");
+    Guard g(idx);
+    if (k <= 0 || min_k < k || min_k > 4096)
+        return fail(idx, SSG_EINVAL, "closest pairs need 0 < k <= min_k <= 4096 (got k = %d, min_k = %d)", k, min_k);
+    if (!out_i || !out_j || !out_d || !count) return fail(idx, SSG_EINVAL, "NULL output pointer");
+    const bool own = host_B == nullptr;  // B is the indexed database itself
+    if (own) {
+        m = idx->n;
+        samedata = 1;
+    }
+    if (m < 0) return fail(idx, SSG_EINVAL, "negative number of objects");
+    for (int32_t r = 0; r < k; ++r) { out_i[r] = 0; out_j[r] = 0; out_d[r] = INFINITY; }
+    *count = 0;
+    const int64_t avail = idx->n - (samedata ? 1 : 0);
+    if (m == 0 || avail <= 0) return SSG_OK;
+    const int kk = int(std::min<int64_t>(min_k, avail));
+    // 1. each object of B: its kk nearest objects of the index (itself excluded)
+    const void *dq;
+    const float *dqn = nullptr;
+    if (own) {
+        dq = idx->db.p;
+        if (idx->metric == SSG_METRIC_COSINE) dqn = static_cast<const float *>(idx->db_norm.p);
+    } else {
+        int rc = prepare_queries(idx, host_B, m, false, &dq, &dqn);
+        if (rc) return rc;
+    }
+    if (int64_t(m) * kk >= (int64_t(1) << 32) - 1) return fail(idx, SSG_EUNSUPPORTED, "too many candidate pairs");
+    SSG_CK(idx->pack_out.ensure(size_t(m) * kk * 8), "allocating pair candidates");
+    uint32_t *ids = static_cast<uint32_t *>(idx->pack_out.p);
+    float *dists = reinterpret_cast<float *>(ids + size_t(m) * kk);
+    int rc = run_knn(idx, dq, dqn, m, kk, samedata ? 1 : 0, ids, dists, own);
+    if (rc) return rc;
+    // 2. the k smallest of the m sorted rows, merged as segments of one list
+    SSG_CK(idx->pack_q.ensure(size_t(m) * kk * 8), "allocating pair keys");
+    uint64_t *keys = static_cast<uint64_t *>(idx->pack_q.p);
+    SSG_CK(ssg::launch_pair_keys(ids, dists, int64_t(m) * kk, keys, idx->stream, &idx->last_launches),
+           "building pair keys");
+    ssg::FinalizeArgs f{};
+    SSG_RC(reduce_segments(idx, keys, 1, int(std::min<int64_t>(m, INT32_MAX)), kk, &f.cand, &f.segs));
+    DevBuf sel;
+    SSG_CK(sel.ensure(size_t(k) * 8 + size_t(k) * 12), "allocating the selection");
+    uint32_t *sel_ids = static_cast<uint32_t *>(sel.p);
+    float *sel_d = reinterpret_cast<float *>(sel_ids + k);
+    f.kk = kk;
+    f.m = 1;
+    f.k_out = k;
+    f.exclude_self = 0;
+    f.self_base = 0;
+    f.out_ids = sel_ids;
+    f.out_dists = sel_d;
+    SSG_CK(ssg::launch_finalize(f, idx->stream, &idx->last_launches), "merging pair candidates");
+    int32_t *di = reinterpret_cast<int32_t *>(sel_d + k);
+    int32_t *dj = di + k;
+    float *dd = reinterpret_cast<float *>(dj + k);
+    SSG_CK(ssg::launch_pair_decode(sel_ids, sel_d, k, ids, kk, di, dj, dd, idx->stream, &idx->last_launches),
+           "decoding pairs");
+    SSG_CK(cudaMemcpyAsync(out_i, di, size_t(k) * 4, cudaMemcpyDeviceToHost, idx->stream), "copying pairs");
+    SSG_CK(cudaMemcpyAsync(out_j, dj, size_t(k) * 4, cudaMemcpyDeviceToHost, idx->stream), "copying pairs");
+    SSG_CK(cudaMemcpyAsync(out_d, dd, size_t(k) * 4, cudaMemcpyDeviceToHost, idx->stream), "copying pairs");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "finding closest pairs");
+    int64_t c = 0;
+    while (c < k && out_i[c] != 0) ++c;
+    *count = c;
+    return SSG_OK;
+}
+
 int ssg_bitsketch(const void *dev_R, int64_t dim, int64_t outdim, const void *dev_X, int64_t n, uint64_t *dev_out,
                   void *stream) {
     if (dim <= 0 || outdim <= 0 || n < 0 || outdim > (int64_t(1) << 24) || dim > (int64_t(1) << 24))

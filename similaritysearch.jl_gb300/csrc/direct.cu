@@ -346,6 +346,47 @@ cudaError_t launch_gather_rows(const void *src, const int64_t *idx, int64_t coun
     return cudaGetLastError();
 }
 
+// Closest pairs.  Row j of (ids, dists) holds object j of B's kk nearest
+// candidates, sorted by (distance, id); pair (ids[j][t], j) gets the key
+// (distance, j * kk + t), so a row is a sorted segment of the global order
+// (distance, j, rank) and the segment merge yields the k closest pairs.
+__global__ void pair_keys_kernel(const uint32_t *__restrict__ ids, const float *__restrict__ dists, int64_t total,
+                                 uint64_t *__restrict__ keys) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x)
+        keys[i] = ids[i] ? make_key(dists[i], uint32_t(i)) : KEY_EMPTY;
+}
+
+// sel_ids / sel_d: the merged top k (1-based flat index + 1, 0 = none)
+__global__ void pair_decode_kernel(const uint32_t *__restrict__ sel_ids, const float *__restrict__ sel_d, int k,
+                                   const uint32_t *__restrict__ ids, int kk, int32_t *__restrict__ oi,
+                                   int32_t *__restrict__ oj, float *__restrict__ od) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    const uint32_t f = sel_ids[r];
+    if (f == 0) { oi[r] = 0; oj[r] = 0; od[r] = INFINITY; return; }
+    const uint32_t flat = f - 1;
+    oi[r] = int32_t(ids[flat]);
+    oj[r] = int32_t(flat / uint32_t(kk)) + 1;
+    od[r] = sel_d[r];
+}
+
+cudaError_t launch_pair_keys(const uint32_t *ids, const float *dists, int64_t total, uint64_t *keys, cudaStream_t st,
+                             int *launches) {
+    if (total <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((total + 255) / 256, 148 * 32);
+    if (launches) *launches += 1;
+    pair_keys_kernel<<<unsigned(blocks), 256, 0, st>>>(ids, dists, total, keys);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pair_decode(const uint32_t *sel_ids, const float *sel_d, int k, const uint32_t *ids, int kk,
+                               int32_t *oi, int32_t *oj, float *od, cudaStream_t st, int *launches) {
+    if (k <= 0) return cudaSuccess;
+    if (launches) *launches += 1;
+    pair_decode_kernel<<<unsigned((k + 127) / 128), 128, 0, st>>>(sel_ids, sel_d, k, ids, kk, oi, oj, od);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, const int64_t *idx, int64_t count,
                                    int k, uint32_t *ids, float *dists, cudaStream_t st, int *launches) {
     if (count <= 0) return cudaSuccess;

@@ -163,6 +163,14 @@ cudaError_t launch_bitsketch(const float *xtiles, const float *rtiles, int64_t d
 cudaError_t launch_gemm_f32(const ScanArgs &a, const float *dtiles, const float *xaux, const float *qtiles,
                             const float *q_norm, cudaStream_t st, int *launches);
 
+// ---- closest pairs (direct.cu) ----
+// keys[j * kk + t] = (dists[j][t], j * kk + t), empty where ids[j][t] == 0
+cudaError_t launch_pair_keys(const uint32_t *ids, const float *dists, int64_t total, uint64_t *keys, cudaStream_t st,
+                             int *launches);
+// (i, j, d) of the merged top k: i = ids[flat], j = flat / kk + 1
+cudaError_t launch_pair_decode(const uint32_t *sel_ids, const float *sel_d, int k, const uint32_t *ids, int kk,
+                               int32_t *oi, int32_t *oj, float *od, cudaStream_t st, int *launches);
+
 // ---- helpers (direct.cu) ----
 // out[i] = sum x^2 per row (sequential FMA) and *max_out = max over rows
 // (max_out must be zeroed first).

@@ -385,3 +385,57 @@ def rerank_b(idx: GPUExhaustiveSearch, queries, knns_ids: np.ndarray, knns_dists
     if od is not knns_dists:
         knns_dists[...] = od
     return knns_ids, knns_dists
+
+
+def bichromatic_kclosestpairs(idx: GPUExhaustiveSearch, ctx: GenericContext, B, k: int = 1, min_k: int | None = None,
+                              samedata: bool | None = None):
+    """The k closest pairs (i in the index, j in B, dist), ascending by
+    distance (src/bichromatic/bichromaticclosestpairs.jl): every object of B
+    takes its min_k nearest indexed objects (itself excluded when
+    ``samedata``, by default when B is the index's own database) and the k
+    best candidates overall are kept.  Ids are 1-based."""
+    min_k = max(k, 8) if min_k is None else min_k
+    if min_k < k:
+        raise ArgumentError("min_k must be >= k")
+    own = B is None or B is idx.db
+    if samedata is None:
+        samedata = own
+    oi = np.zeros(k, dtype=np.int32)
+    oj = np.zeros(k, dtype=np.int32)
+    od = np.zeros(k, dtype=np.float32)
+    cnt = C.c_int64(0)
+    if own:
+        m = len(idx)
+        N.check(N.lib().ssg_closestpairs(idx._h, None, 0, k, min_k, 1, oi.ctypes.data_as(C.c_void_p),
+                                         oj.ctypes.data_as(C.c_void_p), od.ctypes.data_as(C.c_void_p),
+                                         C.byref(cnt)), idx._h)
+    else:
+        rows = idx._queries(B)
+        m = rows.shape[0]
+        N.check(N.lib().ssg_closestpairs(idx._h, rows.ctypes.data_as(C.c_void_p), m, k, min_k, int(bool(samedata)),
+                                         oi.ctypes.data_as(C.c_void_p), oj.ctypes.data_as(C.c_void_p),
+                                         od.ctypes.data_as(C.c_void_p), C.byref(cnt)), idx._h)
+    add_distance_evaluations(ctx, m * len(idx))
+    c = int(cnt.value)
+    return [(int(oi[r]), int(oj[r]), float(od[r])) for r in range(c)]
+
+
+def bichromatic_closestpair(idx: GPUExhaustiveSearch, ctx: GenericContext, B, min_k: int = 8,
+                            samedata: bool | None = None):
+    """The closest pair (i, j, dist) (bichromatic_closestpair); (0, 0, inf)
+    when there is none."""
+    p = bichromatic_kclosestpairs(idx, ctx, B, k=1, min_k=max(1, min_k), samedata=samedata)
+    return p[0] if p else (0, 0, float("inf"))
+
+
+def closestpairs(idx: GPUExhaustiveSearch, ctx: GenericContext, k: int = 1, min_k: int | None = None):
+    """closestpairs(idx, ctx; k, min_k): the k closest pairs among the indexed
+    objects (src/bichromatic/closestpairs.jl)."""
+    return bichromatic_kclosestpairs(idx, ctx, None, k=k, min_k=min_k, samedata=True)
+
+
+def closestpair(idx: GPUExhaustiveSearch, ctx: GenericContext, min_k: int = 8):
+    """closestpair(idx, ctx; min_k): (i, j, dist) of the closest pair among
+    the indexed objects (src/bichromatic/closestpair.jl)."""
+    p = closestpairs(idx, ctx, k=1, min_k=max(2, min_k))
+    return p[0] if p else (0, 0, float("inf"))
