@@ -254,3 +254,53 @@ def closestpairs(metric, A, B, k: int, min_k: int, samedata: bool, lanes: int = 
             cand.append((d, j + 1, r, i))
     cand.sort()
     return [(i, j, d) for d, j, r, i in cand[:k]]
+
+
+def neardup(metric, X, eps: float, blocksize: int = 256, filterblocks: bool = True, lanes: int = 1):
+    """Restates neardup_ / neardup_block! (src/neardup.jl:101-244) with an
+    exact index: returns (nn, dist, map) with 1-based ids.  The search of a
+    block against the net takes the nearest net object (KnnSorted order);
+    inside a block an object joins the net unless the nearest already
+    accepted object of the block (smallest distance, earliest first) is
+    within eps."""
+    X = np.ascontiguousarray(X)
+    n = X.shape[0]
+    eps = np.float32(eps)
+    L = np.zeros(n, dtype=np.int32)
+    D = np.zeros(n, dtype=np.float32)
+    M = []
+
+    def block(imap):
+        keep = [imap[0]] if filterblocks else list(imap)
+        if filterblocks:
+            for i in imap[1:]:
+                best_d, best_j = None, None
+                for j in keep:
+                    d = np.float32(evaluate(metric, X[i], X[j], lanes))
+                    if best_d is None or d < best_d:
+                        best_d, best_j = d, j
+                if best_d > eps:
+                    keep.append(i)
+                else:
+                    L[i], D[i] = best_j + 1, best_d
+        for i in keep:
+            M.append(i + 1)
+            L[i], D[i] = i + 1, 0.0
+
+    blocksize = max(1, min(blocksize, n))
+    for start in range(0, n, blocksize):
+        rng = list(range(start, min(n, start + blocksize)))
+        if not M:
+            block(rng)
+            continue
+        net = X[np.array(M) - 1]
+        ids, dists = searchbatch(metric, net, X[rng], 1, lanes=lanes)
+        imap = []
+        for t, j in enumerate(rng):
+            if dists[t, 0] > eps:
+                imap.append(j)
+            else:
+                L[j], D[j] = M[int(ids[t, 0]) - 1], dists[t, 0]
+        if imap:
+            block(imap)
+    return L, D, np.array(M, dtype=np.uint32)

@@ -6,6 +6,7 @@ sm_103a CUDA library with the C ABI of ``include/ssgpu.h``.
 """
 from . import _native, shard
 from .proj import bitsketch
+from .neardup import neardup
 from .db import AbstractDatabase, MatrixDatabase, MMapMatrixDatabase, VectorDatabase, write_mmap_matrix
 from .dist import Dist, PreMetric, evaluate
 from .index import (ArgumentError, GenericContext, GPUExhaustiveSearch, add_distance_evaluations,
@@ -26,7 +27,7 @@ __all__ = [
     "add_distance_evaluations", "allknn", "allknn_b", "append_items_b", "database", "distance",
     "distance_evaluations", "index_b", "push_item_b", "rerank_b", "search", "searchbatch",
     "searchbatch_b", "searchbatches", "bichromatic_closestpair", "bichromatic_kclosestpairs", "closestpair",
-    "closestpairs", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
+    "closestpairs", "neardup", "LOG", "InformativeLog", "LogList", "RecorderLog", "macrorecall", "recallscore",
     "IdDist", "KnnSorted", "knnqueue", "bitsketch",
 ]
 
