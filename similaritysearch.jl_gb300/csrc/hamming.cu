@@ -25,7 +25,26 @@ constexpr int kDrainTrigger = 4;
 
 template <int WMAX, int QPB>
 __host__ __device__ constexpr size_t ham_static_smem() {
-    return size_t(TN) * WMAX * 8;
+    return size_t(2) * TN * WMAX * 8;  // two sketch tiles: one computed, one landing
+}
+
+// 8-byte asynchronous copy global -> shared, zero-filled when !valid
+__device__ __forceinline__ void cp_async8(uint64_t *dst, const uint64_t *src, bool valid) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+
+// tile of TN sketches starting at row j0 (rows >= hi and words >= W are zeros)
+template <int WMAX, int QPB>
+__device__ __forceinline__ void load_sketches(uint64_t (*xs)[WMAX], const uint64_t *__restrict__ db, int64_t j0,
+                                              int64_t hi, int W) {
+    for (int e = threadIdx.x; e < TN * WMAX; e += QPB) {
+        const int r = e / WMAX, c = e % WMAX;
+        const int64_t xr = j0 + r;
+        const bool v = xr < hi && c < W;
+        cp_async8(&xs[r][c], v ? db + xr * W + c : db, v);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 template <int WMAX, int QPB>
@@ -33,7 +52,7 @@ __global__ void __launch_bounds__(QPB)
 hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__restrict__ Q,
                int heap_in_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
-    uint64_t(*xs)[WMAX] = reinterpret_cast<uint64_t(*)[WMAX]>(smem);
+    uint64_t(*xbuf)[WMAX] = reinterpret_cast<uint64_t(*)[WMAX]>(smem);  // [2 * TN][WMAX]
     uint64_t *hbase = heap_in_smem
         ? reinterpret_cast<uint64_t *>(smem + ham_static_smem<WMAX, QPB>())
         : a.gheap + (size_t(blockIdx.y) * gridDim.x + blockIdx.x) * size_t(a.kk + kBufCap) * QPB;
@@ -52,29 +71,44 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
     BufferedTopK T;
     T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
 
-    for (int64_t j0 = lo; j0 < hi; j0 += TN) {
-        __syncthreads();
-        for (int e = t; e < TN * WMAX; e += QPB) {
-            int r = e / WMAX, c = e % WMAX;
-            int64_t xr = j0 + r;
-            xs[r][c] = (xr < hi && c < W) ? db[xr * W + c] : 0ull;
+    if (lo < hi) load_sketches<WMAX, QPB>(xbuf, db, lo, hi, W);
+    for (int64_t j0 = lo, it = 0; j0 < hi; j0 += TN, ++it) {
+        // the next tile lands while this one is scanned
+        if (j0 + TN < hi) {
+            load_sketches<WMAX, QPB>(xbuf + ((it + 1) & 1) * TN, db, j0 + TN, hi, W);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
+        uint64_t(*xs)[WMAX] = xbuf + (it & 1) * TN;
         const int jn = hi - j0 < TN ? int(hi - j0) : TN;
         for (int g = 0; g < jn; g += 8) {
-            const int ge = g + 8 < jn ? g + 8 : jn;
-            for (int j = g; j < ge; ++j) {
-                int d = 0;
+            // eight rows at once: eight independent XOR + POPC chains per
+            // thread (rows past the end are zero words, filtered below)
+            int d[8];
 #pragma unroll
-                for (int w = 0; w < WMAX; w += 2) {
-                    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(&xs[j][w]);
-                    d += __popcll(q[w] ^ x.x) + __popcll(q[w + 1] ^ x.y);
+            for (int jj = 0; jj < 8; ++jj) d[jj] = 0;
+#pragma unroll
+            for (int w = 0; w < WMAX; w += 2) {
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(&xs[g + jj][w]);
+                    d[jj] += __popcll(q[w] ^ x.x) + __popcll(q[w + 1] ^ x.y);
                 }
-                const float fd = float(d);
-                if (qvalid && fd <= T.topd) T.append(fd, uint32_t(j0 + j + a.id_base));
+            }
+            int dmin = d[0];
+#pragma unroll
+            for (int jj = 1; jj < 8; ++jj) dmin = min(dmin, d[jj]);
+            if (!__any_sync(0xffffffffu, qvalid && float(dmin) <= T.topd)) continue;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const float fd = float(d[jj]);
+                if (qvalid && g + jj < jn && fd <= T.topd) T.append(fd, uint32_t(j0 + g + jj + a.id_base));
             }
             T.maybe_drain(kDrainTrigger);
         }
+        __syncthreads();  // this buffer is refilled two tiles later
     }
     T.drain();
     Heap &H = T.H;
