@@ -126,8 +126,14 @@ bool ham_heap_fits(int kk) {
     return ham_static_smem<WMAX, QPB>() + size_t(kk + kBufCap) * QPB * 8 <= kSmemBudget;
 }
 
+// Queries per block: long candidate lists fill shared memory with heaps, so
+// 64-query blocks (three per SM, six warps) then hide latencies better than
+// one 128-query block (four warps).
 template <int WMAX>
-int ham_qpb(int kk) { return ham_heap_fits<WMAX, 128>(kk) ? 128 : 32; }
+int ham_qpb(int kk) {
+    if (kk >= 48 && ham_heap_fits<WMAX, 64>(kk)) return 64;
+    return ham_heap_fits<WMAX, 128>(kk) ? 128 : 32;
+}
 
 template <int WMAX, int QPB>
 cudaError_t launch_ham_t(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
@@ -143,14 +149,17 @@ cudaError_t launch_ham_t(const ScanArgs &a, const uint64_t *db, const uint64_t *
 
 template <int WMAX>
 cudaError_t launch_ham_w(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
-    return ham_qpb<WMAX>(a.kk) == 128 ? launch_ham_t<WMAX, 128>(a, db, q, st)
-                                      : launch_ham_t<WMAX, 32>(a, db, q, st);
+    const int qpb = ham_qpb<WMAX>(a.kk);
+    if (qpb == 128) return launch_ham_t<WMAX, 128>(a, db, q, st);
+    if (qpb == 64) return launch_ham_t<WMAX, 64>(a, db, q, st);
+    return launch_ham_t<WMAX, 32>(a, db, q, st);
 }
 
 template <int WMAX>
 size_t ham_gheap(const ScanArgs &a) {
     int qpb = ham_qpb<WMAX>(a.kk);
-    bool fits = qpb == 128 ? ham_heap_fits<WMAX, 128>(a.kk) : ham_heap_fits<WMAX, 32>(a.kk);
+    bool fits = qpb == 128 ? ham_heap_fits<WMAX, 128>(a.kk)
+                           : (qpb == 64 ? ham_heap_fits<WMAX, 64>(a.kk) : ham_heap_fits<WMAX, 32>(a.kk));
     if (fits) return 0;
     return size_t((a.m + qpb - 1) / qpb) * a.splits * size_t(a.kk + kBufCap) * qpb * 8;
 }
