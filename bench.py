@@ -335,6 +335,7 @@ def allknn_mode(cx, X, mode, overfetch, steps, warmup):
 
     ms, launches, main_ms, main_launches, clocks = timed_device_steps(cx, h, step, steps, warmup)
     ids_host = ids_d.cpu().numpy().view(np.uint32)
+    dists_host = dists_d.cpu().numpy()
     L.ssg_destroy(h)
     avg = main_ms / max(1, main_launches)
     q_per_launch = n * steps / max(1, main_launches)
@@ -345,7 +346,7 @@ def allknn_mode(cx, X, mode, overfetch, steps, warmup):
         roof["traffic"] = HEADLINE_SCAN_TRAFFIC
         roof["traffic_note"] = "dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of this launch"
     return {"ms_per_step": ms, "qps": cx.world * n / (ms / 1e3), "launches": launches, "roofline": roof,
-            "clocks": clocks, "ids": ids_host}
+            "clocks": clocks, "ids": ids_host, "dists": dists_host}
 
 
 def allknn_e2e(cx, X, mode, overfetch, steps):
@@ -390,6 +391,24 @@ def recall_vs(gold_rows, cids, got):
     return r10, r32
 
 
+def fp64_check(X, got_ids, got_d, rows):
+    """recall@10 / recall@32 against the FP64 oracle (self excluded) and the
+    largest |reported distance - FP64 distance of the same id| on `rows`."""
+    from oracle import oracle as O
+    fi, _ = O.searchbatch_f64("normcosine", X, X[rows], K + 1, nthreads=os.cpu_count() or 1)
+    gold = np.array([[i for i in fi[r] if i != j + 1][:K] for r, j in enumerate(rows)], dtype=np.uint32)
+    g = got_ids[rows]
+    r10 = float(np.mean([len(set(gold[r, :10]) & set(g[r, :10])) / 10 for r in range(rows.size)]))
+    r32 = float(np.mean([len(set(gold[r]) & set(g[r])) / K for r in range(rows.size)]))
+    dmax = 0.0
+    for r, j in enumerate(rows):
+        for t in range(K):
+            i = int(g[r, t])
+            if i:
+                dmax = max(dmax, abs(float(got_d[j, t]) - O.evaluate_f64("normcosine", X[i - 1], X[j])))
+    return {"recall@10": r10, "recall@32": r32, "max_abs_ddist": dmax, "sample_rows": int(rows.size)}
+
+
 def gpu_arm(args):
     cx = Ctx()
     X = make_mixture(N_DB)
@@ -415,6 +434,7 @@ def gpu_arm(args):
         return
     cpu, rows, cids, _ = cpu_baseline(X, budget_s=args.cpu_budget)
     r10, r32 = recall_vs(rows, cids, head["ids"])
+    f64 = fp64_check(X, head["ids"], head["dists"], rows[:256])
     modes[mode]["recall@10"], modes[mode]["recall@32"] = r10, r32
     if plain is not None:
         p10, p32 = recall_vs(rows, cids, plain["ids"])
@@ -426,7 +446,7 @@ def gpu_arm(args):
         "vs_baseline": None, "dtype": "f32" if mode == "fp32" else mode, "data": DATA,
         "config": config_dict(mode, of),
         "recall": {"recall@10": r10, "recall@32": r32, "sample_rows": int(rows.size),
-                   "gold": "oracle ExhaustiveSearch restatement (FP32, 16-lane sums)"},
+                   "gold": "oracle ExhaustiveSearch restatement (FP32, 16-lane sums)", "vs_fp64": f64},
         "roofline": head["roofline"],
         "cpu_baseline": {k: v for k, v in cpu.items() if k != "seconds"},
         "e2e": e2e,
@@ -497,6 +517,12 @@ def workload_arm(args):
         # one pass over the sketches + the queries + the results (bytes per call)
         roof = roofline_bytes(8.0 * d * n + 8.0 * d * m + 8.0 * k * m, avg)
         roof["popcount_words_per_s"] = n * m * d / (avg / 1e3)
+        # the binding roof at m = 1e4: 64-bit XOR + POPC issue, 16 32-bit
+        # POPC per clock per SM = 8 words per clock per SM (nominal, at the
+        # measured maximum SM clock; no measured INT peak exists)
+        words_peak = 152 * 8 * peaks().get("sm_max_mhz", 2070.0) * 1e6
+        roof["popcount_peak_words_per_s"] = words_peak
+        roof["popcount_frac"] = roof["popcount_words_per_s"] / words_peak
     # e2e: create from host + search from host + results to host
     Xp = torch.from_numpy(X.view(np.int64) if X.dtype == np.uint64 else X).pin_memory()
     Qp = torch.from_numpy(Q.view(np.int64) if Q.dtype == np.uint64 else Q).pin_memory()
