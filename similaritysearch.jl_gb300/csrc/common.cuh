@@ -42,6 +42,26 @@ __host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
     return f;
 }
 
+// Three-operand minimum / maximum (one instruction on sm_100+; NaN operands
+// are ignored like fminf / fmaxf do).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+// minimum / maximum of 8 values in 4 instructions
+__device__ __forceinline__ float fmin8(const float *v) {
+    return fmin3(fmin3(v[0], v[1], v[2]), fmin3(v[3], v[4], v[5]), fminf(v[6], v[7]));
+}
+__device__ __forceinline__ float fmax8(const float *v) {
+    return fmax3(fmax3(v[0], v[1], v[2]), fmax3(v[3], v[4], v[5]), fmaxf(v[6], v[7]));
+}
+
 __host__ __device__ __forceinline__ uint64_t make_key(float d, uint32_t id0) {
     return (static_cast<uint64_t>(float_to_ordered(d)) << 32) | id0;
 }

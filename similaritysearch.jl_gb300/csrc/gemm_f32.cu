@@ -260,8 +260,7 @@ gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const fl
                 for (int c = 0; c < BN; c += 8) {
                     const float4 v0 = *reinterpret_cast<const float4 *>(row + c);
                     const float4 v1 = *reinterpret_cast<const float4 *>(row + c + 4);
-                    const float gm = fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)),
-                                           fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w)));
+                    const float gm = fmin3(fmin3(v0.x, v0.y, v0.z), fmin3(v0.w, v1.x, v1.y), fminf(v1.z, v1.w));
                     if (!__any_sync(0xffffffffu, gm <= (row_valid ? T.topd : -INFINITY))) continue;
                     const float vv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll

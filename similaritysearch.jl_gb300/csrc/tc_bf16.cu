@@ -317,18 +317,15 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                 float dv[32];
                 float gmin[4];
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    float m = MC == MC_DOT ? -INFINITY : INFINITY;
-#pragma unroll
-                    for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                        const float v = __uint_as_float(r[c][j]);
-                        if (MC == MC_DOT) { dv[j] = v; m = fmaxf(m, v); }
-                        else if (MC == MC_SQ) { dv[j] = fmaf(-2.0f, v, __ldg(nrm + j)); m = fminf(m, dv[j]); }
-                        else { dv[j] = -v * __ldg(nrm + j); m = fminf(m, dv[j]); }
-                    }
-                    gmin[g] = MC == MC_DOT ? -m : m;
+                for (int j = 0; j < 32; ++j) {
+                    const float v = __uint_as_float(r[c][j]);
+                    if (MC == MC_DOT) dv[j] = v;
+                    else if (MC == MC_SQ) dv[j] = fmaf(-2.0f, v, __ldg(nrm + j));
+                    else dv[j] = -v * __ldg(nrm + j);
                 }
-                const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+#pragma unroll
+                for (int g = 0; g < 4; ++g) gmin[g] = MC == MC_DOT ? -fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
+                const float dmin = fmin3(fmin3(gmin[0], gmin[1], gmin[2]), gmin[3], gmin[3]);
                 if (FILTER) {
                     // rare: ~3 * kk of the n columns pass a query's threshold
                     if (__any_sync(0xffffffffu, dmin <= topd)) {

@@ -385,16 +385,11 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                 float dv[32];
                 float gmin[4];
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    float mn = INFINITY;
+                for (int j = 0; j < 32; ++j)
+                    dv[j] = fmaf(__uint_as_float(r[c][j]) * gamma, __ldg(al + j), __ldg(be + j));
 #pragma unroll
-                    for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                        dv[j] = fmaf(__uint_as_float(r[c][j]) * gamma, __ldg(al + j), __ldg(be + j));
-                        mn = fminf(mn, dv[j]);
-                    }
-                    gmin[g] = mn;
-                }
-                const float dmin = fminf(fminf(gmin[0], gmin[1]), fminf(gmin[2], gmin[3]));
+                for (int g = 0; g < 4; ++g) gmin[g] = fmin8(dv + 8 * g);
+                const float dmin = fmin3(fmin3(gmin[0], gmin[1], gmin[2]), gmin[3], gmin[3]);
                 if (shared && sb.cbest) {
                     // best candidates seen, padding rows of the last tile excluded
                     if (sb.cbest == 1 && id0 + 32 <= a.n) {
