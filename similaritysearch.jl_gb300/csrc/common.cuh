@@ -189,19 +189,26 @@ struct BufferedTopK {
     }
 };
 
-// Drains the c keys buffered at buf (stride st) into the heap h and returns
-// the new top.  All 32 lanes of the warp call it together, so the lanes'
+// Drains the c entries buffered at buf (stride st) into the heap h and
+// returns the new top.  All 32 lanes of the warp call it together, so the lanes'
 // sift-downs run side by side.  Kept out of line so a kernel carries one copy
 // of the heap loop however many call sites it has (large unrolled epilogues
 // otherwise overflow the instruction cache); every argument is a scalar, so
 // the call needs no stack.
-static __device__ __noinline__ uint64_t heap_drain(uint64_t *h, const uint64_t *buf, int kk, int st, int c,
-                                            uint64_t top) {
+// Each slot holds a raw append: the 0-based id in its high word and the bits
+// of the column's value in its low word; the value is the distance, or its
+// negation when NEG.  The key is made here, once per candidate, instead of
+// once per appended column.
+template <bool NEG>
+static __device__ __noinline__ uint64_t heap_drain_raw(uint64_t *h, const uint64_t *buf, int kk, int st, int c,
+                                                       uint64_t top) {
     const int cmax = __reduce_max_sync(0xffffffffu, c);
     Heap H{h, kk, st};
     for (int r = 0; r < cmax; ++r) {
         if (r < c) {
-            const uint64_t key = buf[r * st];
+            const uint64_t raw = buf[r * st];
+            const float v = __uint_as_float(static_cast<uint32_t>(raw));
+            const uint64_t key = make_key(NEG ? -v : v, static_cast<uint32_t>(raw >> 32));
             if (key < top) top = H.replace_top(key);
         }
     }

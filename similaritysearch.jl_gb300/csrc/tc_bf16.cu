@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         const bool warp_live = (int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
         uint64_t top = KEY_EMPTY;
         float topd = qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
+        float ntopd = -topd;
         int nbuf = 0;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
             const int b = t % NACC;
@@ -312,10 +313,11 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             for (int c = 0; c < CHUNKS; ++c) {
                 const int64_t id0 = row0 + c * 32;
                 const float *nrm = a.dnorm + id0;
-                // approximate distance of each column and its minimum per
-                // group of 8 columns (DOT ranks by -v: take the maximum of v)
+                // approximate distance of each column and the best per group
+                // of 8 columns.  DOT ranks by -v: its columns keep v, take the
+                // maximum and compare with -topd (exact: negation is exact)
                 float dv[32];
-                float gmin[4];
+                float gbest[4];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const float v = __uint_as_float(r[c][j]);
@@ -324,15 +326,18 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                     else dv[j] = -v * __ldg(nrm + j);
                 }
 #pragma unroll
-                for (int g = 0; g < 4; ++g) gmin[g] = MC == MC_DOT ? -fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
-                const float dmin = fmin3(fmin3(gmin[0], gmin[1], gmin[2]), gmin[3], gmin[3]);
+                for (int g = 0; g < 4; ++g) gbest[g] = MC == MC_DOT ? fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
+                const float cbest = MC == MC_DOT ? fmax3(fmax3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3])
+                                                 : fmin3(fmin3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3]);
+                // x is at or below the query's bound
+                auto passes = [&](float x) { return MC == MC_DOT ? x >= ntopd : x <= topd; };
                 if (FILTER) {
                     // rare: ~3 * kk of the n columns pass a query's threshold
-                    if (__any_sync(0xffffffffu, dmin <= topd)) {
+                    if (__any_sync(0xffffffffu, passes(cbest))) {
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
-                            const float d = MC == MC_DOT ? -dv[j] : dv[j];
-                            if (d <= topd && id0 + j < a.n) {
+                            if (passes(dv[j]) && id0 + j < a.n) {
+                                const float d = MC == MC_DOT ? -dv[j] : dv[j];
                                 const int pos = atomicAdd(a.fcount + query, 1);
                                 if (pos < a.fcap) a.fout[size_t(query) * a.fcap + pos] = make_key(d, uint32_t(id0 + j));
                             }
@@ -340,28 +345,31 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                     }
                     continue;
                 }
-                if (__any_sync(0xffffffffu, dmin <= topd)) {
+                if (__any_sync(0xffffffffu, passes(cbest))) {
+                    const int lim = int(id0 + 32 <= a.n ? 32 : a.n - id0);  // valid columns
 #pragma unroll
                     for (int g = 0; g < 4; ++g) {
-                        if (!__any_sync(0xffffffffu, gmin[g] <= topd)) continue;
+                        if (!__any_sync(0xffffffffu, passes(gbest[g]))) continue;
 #pragma unroll
                         for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                            // branch-free append: the slot is always written,
-                            // the count only advances for a candidate
-                            const float d = MC == MC_DOT ? -dv[j] : dv[j];
-                            cbuf[nbuf * hs] = make_key(d, uint32_t(id0 + j));
-                            nbuf += (d <= topd && id0 + j < a.n) ? 1 : 0;
+                            // branch-free raw append: the slot is always
+                            // written (the id and the column's value; the key
+                            // is made when the buffer drains), the count only
+                            // advances for a candidate
+                            cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
+                            nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
                         }
                         if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
-                            top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+                            top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top);
                             nbuf = 0;
                             topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                            ntopd = -topd;
                         }
                     }
                 }
             }
         }
-        if (!FILTER) top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        if (!FILTER) top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top);
         Heap H{heap, a.kk, hs};
         if (!FILTER && query < a.m) {
             H.sort_ascending();

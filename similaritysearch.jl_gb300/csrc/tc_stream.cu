@@ -401,16 +401,19 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
                     }
                 }
                 if (__any_sync(0xffffffffu, dmin <= topd)) {
+                    const int lim = int(id0 + 32 <= a.n ? 32 : a.n - id0);  // valid columns
 #pragma unroll
                     for (int g = 0; g < 4; ++g) {
                         if (!__any_sync(0xffffffffu, gmin[g] <= topd)) continue;
 #pragma unroll
                         for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                            cbuf[nbuf * hs] = make_key(dv[j], uint32_t(id0 + j));
-                            nbuf += (dv[j] <= topd && id0 + j < a.n) ? 1 : 0;
+                            // raw append (id, distance bits): the key is made
+                            // when the buffer drains, once per candidate
+                            cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
+                            nbuf += (dv[j] <= topd && j < lim) ? 1 : 0;
                         }
                         if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
-                            top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+                            top = heap_drain_raw<false>(heap, cbuf, a.kk, hs, nbuf, top);
                             nbuf = 0;
                             topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
                             if (shared) {
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(st_threads<CS>(), 1) tc_stream_kernel(StreamAr
             if (shared) sb.checkpoint(t + 1, false);
         }
         if (shared) sb.checkpoint(T_tiles, true);
-        if (warp_live) top = heap_drain(heap, cbuf, a.kk, hs, nbuf, top);
+        if (warp_live) top = heap_drain_raw<false>(heap, cbuf, a.kk, hs, nbuf, top);
         Heap H{heap, a.kk, hs};
         if (warp_live && query < a.m) {
             H.sort_ascending();
