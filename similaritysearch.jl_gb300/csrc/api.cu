@@ -77,6 +77,12 @@ struct ssg_index {
     // BF16 tensor-core mode: operand tiles of the database and the queries,
     // per-row norms of the padded database, and the device status word.
     DevBuf tc_db, tc_norm, tc_q, status;
+    // allknn's locality order (tc_bf16.cu): position -> id, start tile of
+    // each query tile's scan, BF16 tiles and norms in that order; built for
+    // loc_n rows (-1: none)
+    DevBuf loc_perm, loc_rot, loc_tiles, loc_norm;
+    int64_t loc_n = -1;
+    int locality_param = 1;
     // K-streaming tensor-core path (FP8 mode, and BF16 for dim > 256): operand
     // tiles, per-row FP8 scales, per-row epilogue coefficients, query tiles
     DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
@@ -224,6 +230,7 @@ int ensure_db_capacity(ssg_index *idx, int64_t rows) {
 // Tiles are allocated in pairs so a CTA holding two query tiles never reads
 // past the end when the database doubles as the query set (allknn).
 int build_tc_tiles(ssg_index *idx) {
+    idx->loc_n = -1;
     const int64_t tiles = (ssg::tc_tiles(idx->n) + 1) / 2 * 2;
     const size_t tb = ssg::tc_tile_bytes(idx->dim);
     SSG_CK(idx->tc_db.ensure(size_t(tiles) * tb), "allocating BF16 database tiles");
@@ -695,6 +702,78 @@ int64_t overfetch_kk(const ssg_index *idx, int take) {
     return std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
 }
 
+// allknn's locality order needs at least this many rows (below it the order's
+// set-up would cost more than the heap insertions it saves)
+constexpr int64_t kLocalityMinRows = 32768;
+
+// Builds allknn's locality order (tc_bf16.cu, launch_locality_order): P
+// evenly spaced rows as pivots (about 1024 rows per pivot), each row's
+// nearest pivot by a kk = 1 scan of the BF16 tiles against the pivots' tiles,
+// rows grouped by pivot, and the BF16 tiles and norms rebuilt in that order.
+// Kept until the database changes.
+int ensure_locality(ssg_index *idx) {
+    if (idx->loc_n == idx->n) return SSG_OK;
+    const int64_t n = idx->n;
+    const int P = int(std::min<int64_t>(16384, std::max<int64_t>(128, (n / 1024 + 127) / 128 * 128)));
+    std::vector<uint32_t> prow(static_cast<size_t>(P));
+    for (int i = 0; i < P; ++i) prow[size_t(i)] = uint32_t(int64_t(i) * n / P);
+    const size_t tb = ssg::tc_tile_bytes(idx->dim);
+    const int64_t ptiles = (ssg::tc_tiles(P) + 1) / 2 * 2;
+    const int segs = ssg::tc_segments_per_split(1);
+    DevBuf prow_d, pt, pn, work;
+    SSG_CK(prow_d.ensure(size_t(P) * 4), "allocating the pivot list");
+    SSG_CK(cudaMemcpyAsync(prow_d.p, prow.data(), size_t(P) * 4, cudaMemcpyHostToDevice, idx->stream),
+           "copying the pivot list");
+    SSG_CK(pt.ensure(size_t(ptiles) * tb), "allocating pivot tiles");
+    SSG_CK(pn.ensure(size_t(ptiles) * 128 * 4), "allocating pivot norms");
+    const float *x = static_cast<const float *>(idx->db.p);
+    const uint32_t *pmap = static_cast<const uint32_t *>(prow_d.p);
+    SSG_CK(ssg::launch_bf16_tiles(x, P, idx->dim, ptiles, static_cast<uint8_t *>(pt.p), idx->stream,
+                                  &idx->last_launches, pmap),
+           "building pivot tiles");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, x, P, idx->dim, ptiles * 128, static_cast<float *>(pn.p), idx->stream,
+                                &idx->last_launches, pmap),
+           "computing pivot norms");
+    // nearest pivot of every row (its keys), then per-row pivot, bucket
+    // counts, starts and cursors in one scratch buffer
+    const size_t cand_bytes = size_t(n) * segs * 8;
+    SSG_CK(work.ensure(cand_bytes + size_t(n) * 4 + size_t(P) * 12), "allocating locality scratch");
+    uint64_t *cand = static_cast<uint64_t *>(work.p);
+    uint32_t *pivot = reinterpret_cast<uint32_t *>(static_cast<char *>(work.p) + cand_bytes);
+    int *count = reinterpret_cast<int *>(pivot + n);
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    SSG_CK(ssg::launch_tc_scan(idx->metric, static_cast<const uint8_t *>(idx->tc_db.p),
+                               static_cast<const uint8_t *>(pt.p), static_cast<const float *>(pn.p), P, n, idx->dim,
+                               1, 1, cand, static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches,
+                               nullptr),
+           "launching the pivot scan");
+    const int64_t qtiles = ssg::tc_tiles(n);
+    SSG_CK(idx->loc_perm.ensure(size_t(n) * 4), "allocating the locality order");
+    SSG_CK(idx->loc_rot.ensure(size_t(qtiles) * 4), "allocating scan start tiles");
+    uint32_t *perm = static_cast<uint32_t *>(idx->loc_perm.p);
+    SSG_CK(ssg::launch_locality_order(cand, n, segs, P, pivot, count, count + P, count + 2 * P, perm,
+                                      static_cast<int *>(idx->loc_rot.p), idx->stream, &idx->last_launches),
+           "ordering rows by pivot");
+    const int64_t tiles = (qtiles + 1) / 2 * 2;
+    SSG_CK(idx->loc_tiles.ensure(size_t(tiles) * tb), "allocating locality-ordered tiles");
+    SSG_CK(ssg::launch_bf16_tiles(x, n, idx->dim, tiles, static_cast<uint8_t *>(idx->loc_tiles.p), idx->stream,
+                                  &idx->last_launches, perm),
+           "building locality-ordered tiles");
+    SSG_CK(idx->loc_norm.ensure(size_t(tiles) * 128 * 4), "allocating locality-ordered norms");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, x, n, idx->dim, tiles * 128, static_cast<float *>(idx->loc_norm.p),
+                                idx->stream, &idx->last_launches, perm),
+           "computing locality-ordered norms");
+    int status = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building the locality order");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the pivot scan gave up (code %d)", status);
+    idx->loc_n = n;
+    return SSG_OK;
+}
+
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db) {
     const int take = k + (exclude_self ? 1 : 0);
@@ -725,6 +804,19 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
     const size_t tb = ssg::tc_tile_bytes(idx->dim);
     const uint8_t *qtiles = static_cast<const uint8_t *>(idx->tc_db.p);
+    const uint8_t *dtiles = static_cast<const uint8_t *>(idx->tc_db.p);
+    const float *dnorm = static_cast<const float *>(idx->tc_norm.p);
+    const uint32_t *perm = nullptr;
+    const int *rot = nullptr;
+    // allknn in one launch: scan the database in its locality order
+    if (queries_are_db && idx->locality_param && !idx->capturing && m == idx->n && idx->n >= kLocalityMinRows &&
+        chunk >= m && qt == 1) {
+        SSG_RC(ensure_locality(idx));
+        qtiles = dtiles = static_cast<const uint8_t *>(idx->loc_tiles.p);
+        dnorm = static_cast<const float *>(idx->loc_norm.p);
+        perm = static_cast<const uint32_t *>(idx->loc_perm.p);
+        rot = static_cast<const int *>(idx->loc_rot.p);
+    }
     if (!queries_are_db) {
         const int64_t qt_alloc = (m + qrows - 1) / qrows * qt;
         SSG_CK(idx->tc_q.ensure(size_t(qt_alloc) * tb), "allocating BF16 query tiles");
@@ -736,11 +828,10 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     for (int64_t c0 = 0; c0 < m; c0 += chunk) {
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
-        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb,
-                                   static_cast<const uint8_t *>(idx->tc_db.p),
-                                   static_cast<const float *>(idx->tc_norm.p), idx->n, mc, idx->dim, kk, int(splits),
-                                   static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
-                                   idx->stream, &idx->last_launches, nullptr),
+        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, idx->dim,
+                                   kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
+                                   static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
+                                   perm, rot),
                "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
@@ -1552,6 +1643,8 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
     } else if (k == "graphs") {
         idx->graphs_param = value != 0.0;
         if (!idx->graphs_param) clear_graphs(idx);
+    } else if (k == "locality") {
+        idx->locality_param = value != 0.0;
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -1572,6 +1665,7 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "splits") *value = idx->splits_param;
     else if (k == "overfetch") *value = idx->overfetch;
     else if (k == "profile") *value = idx->profile;
+    else if (k == "locality") *value = idx->locality_param;
     else if (k == "graphs") *value = idx->graphs_param;
     else if (k == "graph_replays") *value = double(idx->graph_replays);
     else if (k == "last_graph") *value = idx->last_graph;
@@ -1800,6 +1894,7 @@ void ssg_destroy(ssg_index *idx) {
     idx->tc_norm.release();
     idx->tc_q.release();
     idx->status.release();
+    for (DevBuf *b : {&idx->loc_perm, &idx->loc_rot, &idx->loc_tiles, &idx->loc_norm}) b->release();
     ssg::learned_free(idx->learned);
     idx->learned = nullptr;
     for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale,

@@ -198,17 +198,19 @@ struct BufferedTopK {
 // Each slot holds a raw append: the 0-based id in its high word and the bits
 // of the column's value in its low word; the value is the distance, or its
 // negation when NEG.  The key is made here, once per candidate, instead of
-// once per appended column.
+// once per appended column.  With a map, the high word is a position and the
+// key takes the id map[position].
 template <bool NEG>
 static __device__ __noinline__ uint64_t heap_drain_raw(uint64_t *h, const uint64_t *buf, int kk, int st, int c,
-                                                       uint64_t top) {
+                                                       uint64_t top, const uint32_t *map = nullptr) {
     const int cmax = __reduce_max_sync(0xffffffffu, c);
     Heap H{h, kk, st};
     for (int r = 0; r < cmax; ++r) {
         if (r < c) {
             const uint64_t raw = buf[r * st];
             const float v = __uint_as_float(static_cast<uint32_t>(raw));
-            const uint64_t key = make_key(NEG ? -v : v, static_cast<uint32_t>(raw >> 32));
+            const uint32_t pos = static_cast<uint32_t>(raw >> 32);
+            const uint64_t key = make_key(NEG ? -v : v, map ? map[pos] : pos);
             if (key < top) top = H.replace_top(key);
         }
     }

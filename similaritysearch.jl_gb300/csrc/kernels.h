@@ -103,16 +103,29 @@ bool tc_choose(int kp, int kk, int *qt, int *stages);
 // Sorted candidate segments the scan writes per (query, split) for a CTA with
 // `qt` query tiles (the epilogue splits a tile's columns between warps).
 int tc_segments_per_split(int qt);
+// With a map, tile row i holds source row map[i].
 cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
-                              cudaStream_t st, int *launches);
-// |x|^2 (SqL2/L2) or 1/|x| (Cosine) per padded row.
+                              cudaStream_t st, int *launches, const uint32_t *map = nullptr);
+// |x|^2 (SqL2/L2) or 1/|x| (Cosine) per padded row (of source row map[i]
+// with a map).
 cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,
-                            cudaStream_t st, int *launches);
+                            cudaStream_t st, int *launches, const uint32_t *map = nullptr);
 // The fused scan: per (query, split) the kk best approximate keys.  *err is
-// set non-zero if a bounded wait gave up.
+// set non-zero if a bounded wait gave up.  With perm / rot (allknn over
+// tiles built in a locality order, one launch for all queries): perm[p] is
+// the id of the row at position p of both tile sets, query CTA x starts at
+// database tile rot[x], keys carry ids and each query's candidates go to
+// the row of its id.
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
-                           cudaStream_t st, int *launches, int *qt_out);
+                           cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm = nullptr,
+                           const int *rot = nullptr);
+// Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
+// segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
+// grouped by pivot) and rot (start tile of each query tile's scan).
+cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, uint32_t *pivot, int *count,
+                                  int *start, int *cursor, uint32_t *perm, int *rot, cudaStream_t st,
+                                  int *launches);
 // Threshold-filter scan for candidate counts beyond the on-chip heaps: every
 // (query, row) with d~ <= thr[query] is appended to the query's fcap-key list.
 cudaError_t launch_tc_filter(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,

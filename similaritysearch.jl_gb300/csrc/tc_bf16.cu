@@ -79,8 +79,10 @@ int metric_class(int metric) {
 // ---------------------------------------------------------------------------
 // Prep: FP32 rows -> BF16 tiles in the swizzled operand layout.
 // ---------------------------------------------------------------------------
+// Tile row i holds source row map[i] when a map is given (a reordering of the
+// database), row i otherwise.
 __global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kp, int64_t tiles,
-                                 uint8_t *__restrict__ out) {
+                                 const uint32_t *__restrict__ map, uint8_t *__restrict__ out) {
     const int chunks_per_row = kp / 8;
     const int64_t total = tiles * TILE * chunks_per_row;
     const size_t tile_bytes = size_t(TILE) * kp * 2;
@@ -92,10 +94,11 @@ __global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int 
         const int r = int(grow % TILE);
         const int col0 = cidx * 8;
         __align__(16) __nv_bfloat16 v[8];
+        const int64_t src = grow < rows && map ? int64_t(map[grow]) : grow;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             float f = 0.0f;
-            if (grow < rows && col0 + e < dim) f = x[grow * dim + col0 + e];
+            if (grow < rows && col0 + e < dim) f = x[src * dim + col0 + e];
             v[e] = __float2bfloat16_rn(f);
         }
         const int blk = col0 / KBE;
@@ -107,12 +110,12 @@ __global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int 
 
 // Per padded row: |x|^2 (MC_SQ) or 1/|x| (MC_COS), 0 for padding rows.
 __global__ void tc_norm_kernel(const float *__restrict__ x, int64_t rows, int dim, int64_t padded, int mc,
-                               float *__restrict__ out) {
+                               const uint32_t *__restrict__ map, float *__restrict__ out) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= padded) return;
     float s = 0.0f;
     if (i < rows) {
-        const float *r = x + i * dim;
+        const float *r = x + (map ? int64_t(map[i]) : i) * dim;
         for (int c = 0; c < dim; ++c) s = fmaf(r[c], r[c], s);
     }
     out[i] = (mc == MC_COS) ? (s > 0.0f ? 1.0f / sqrtf(s) : 0.0f) : s;
@@ -141,6 +144,12 @@ struct TcArgs {
     uint64_t *fout;
     int *fcount;
     int fcap;
+    // locality order (allknn over a reordered database, heap mode only):
+    // perm[p] = the 0-based id of the row at position p of the query and
+    // database tiles; query CTA x starts its scan at database tile rot[x]
+    // and wraps around.  Null: identity order, no rotation.
+    const uint32_t *perm;
+    const int *rot;
 };
 
 template <int QT, int STAGES>
@@ -211,6 +220,12 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
     int64_t t_hi = t_lo + a.split_tiles;
     if (t_hi > a.n_tiles) t_hi = a.n_tiles;
     const int T_tiles = t_hi > t_lo ? int(t_hi - t_lo) : 0;
+    // database tile of the CTA's t-th step: t_lo + t, rotated by rot[x]
+    const int64_t rot = a.rot ? int64_t(a.rot[blockIdx.x]) : 0;
+    auto phys_tile = [&](int t) {
+        int64_t p = t_lo + t + rot;
+        return p >= a.n_tiles ? p - a.n_tiles : p;
+    };
 
     if (warp == 0) {
         if (lane == 0) {
@@ -224,7 +239,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                 const uint32_t ph = (t / STAGES) & 1;
                 if (!tc::mbar_wait(&empty[s], ph ^ 1, a.err, 1)) break;
                 tc::mbar_arrive_expect_tx(&full[s], uint32_t(tile_bytes));
-                tc::bulk_g2s(sB + s * tile_bytes, a.dt + size_t(t_lo + t) * tile_bytes, uint32_t(tile_bytes),
+                tc::bulk_g2s(sB + s * tile_bytes, a.dt + size_t(phys_tile(t)) * tile_bytes, uint32_t(tile_bytes),
                              &full[s]);
                 issued = t + 1;
             }
@@ -296,7 +311,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
-            const int64_t row0 = (t_lo + t) * TILE + cs * (TILE / CS);
+            const int64_t row0 = phys_tile(t) * TILE + cs * (TILE / CS);
             // this warp's columns in flight together, one wait, then the
             // accumulator goes back to the MMA warp before any filtering
             uint32_t r[CHUNKS][32];
@@ -360,7 +375,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                             nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
                         }
                         if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
-                            top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top);
+                            top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top, a.perm);
                             nbuf = 0;
                             topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
                             ntopd = -topd;
@@ -369,11 +384,13 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                 }
             }
         }
-        if (!FILTER) top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top);
+        if (!FILTER) top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top, a.perm);
         Heap H{heap, a.kk, hs};
         if (!FILTER && query < a.m) {
             H.sort_ascending();
-            uint64_t *out = a.cand + ((size_t(query) * a.splits + blockIdx.y) * CS + cs) * a.kk;
+            // the candidates of a query go to its row by id
+            const size_t qrow = a.perm ? size_t(a.perm[query]) : size_t(query);
+            uint64_t *out = a.cand + ((qrow * a.splits + blockIdx.y) * CS + cs) * a.kk;
             for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
         }
     }
@@ -444,6 +461,76 @@ __global__ void filter_select_kernel(const uint64_t *__restrict__ fout, const in
     for (int i = threadIdx.x; i < kk; i += blockDim.x) out[i] = sk[i];
 }
 
+// ---------------------------------------------------------------------------
+// Locality order for allknn.  Rows are grouped by their nearest pivot (P
+// evenly spaced database rows), so a query tile's near neighbours sit in a
+// few consecutive database tiles, and each query CTA starts its scan there.
+// The heaps then hold close candidates after a few tiles and later tiles
+// rarely pass the frontier: far fewer heap insertions than in id order,
+// where the frontier only tightens as ~kk * ln(columns seen).  The kept
+// (distance, id) keys, and so the results, do not depend on the order.
+// ---------------------------------------------------------------------------
+// pivot[i] = position (0..P-1) of row i's best pivot among its segment keys
+// (a kk = 1 scan of the rows against the pivots); count[pivot] += 1
+__global__ void nearest_pivot_kernel(const uint64_t *__restrict__ cand, int64_t n, int segs,
+                                     uint32_t *__restrict__ pivot, int *__restrict__ count) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t best = KEY_EMPTY;
+    for (int s = 0; s < segs; ++s) best = min(best, cand[size_t(i) * segs + s]);
+    const uint32_t p = best == KEY_EMPTY ? 0u : key_id0(best);
+    pivot[i] = p;
+    atomicAdd(count + p, 1);
+}
+
+// start[b] = first position of bucket b (exclusive prefix sum of count), one
+// block; cursor = a copy for the scatter
+__global__ void bucket_offsets_kernel(const int *__restrict__ count, int P, int *__restrict__ start,
+                                      int *__restrict__ cursor) {
+    __shared__ int part[1024];
+    const int per = (P + int(blockDim.x) - 1) / int(blockDim.x);
+    const int lo = int(threadIdx.x) * per;
+    const int hi = min(P, lo + per);
+    int sum = 0;
+    for (int i = lo; i < hi; ++i) sum += count[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int t = 0; t < int(blockDim.x); ++t) {
+            const int v = part[t];
+            part[t] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    int acc = part[threadIdx.x];
+    for (int i = lo; i < hi; ++i) {
+        start[i] = acc;
+        cursor[i] = acc;
+        acc += count[i];
+    }
+}
+
+// perm[position] = row, rows grouped by bucket (the order inside a bucket is
+// whatever the atomics give: the results do not depend on it)
+__global__ void bucket_scatter_kernel(const uint32_t *__restrict__ pivot, int64_t n, int *__restrict__ cursor,
+                                      uint32_t *__restrict__ perm) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int pos = atomicAdd(cursor + pivot[i], 1);
+    perm[pos] = uint32_t(i);
+}
+
+// rot[x] = the database tile where query tile x's scan starts: the tile
+// holding the first position of the bucket of the tile's first row
+__global__ void scan_rotation_kernel(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ pivot,
+                                     const int *__restrict__ start, int64_t qtiles, int *__restrict__ rot) {
+    const int64_t x = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (x >= qtiles) return;
+    rot[x] = start[pivot[perm[x * TILE]]] / TILE;
+}
+
 constexpr size_t kMaxSmem = 227 * 1024;
 
 }  // namespace
@@ -468,22 +555,22 @@ bool tc_choose(int kp, int kk, int *qt, int *stages) {
 }
 
 cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
-                              cudaStream_t st, int *launches) {
+                              cudaStream_t st, int *launches, const uint32_t *map) {
     const int kp = tc_padded_k(dim);
     const int64_t total = tiles * TILE * (kp / 8);
     int64_t blocks = (total + 255) / 256;
     if (blocks > 148 * 64) blocks = 148 * 64;
     if (blocks < 1) blocks = 1;
     if (launches) *launches += 1;
-    bf16_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kp, tiles, out);
+    bf16_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kp, tiles, map, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,
-                            cudaStream_t st, int *launches) {
+                            cudaStream_t st, int *launches, const uint32_t *map) {
     const int mc = metric_class(metric);
     if (launches) *launches += 1;
-    tc_norm_kernel<<<unsigned((padded + 255) / 256), 256, 0, st>>>(x, rows, int(dim), padded, mc, out);
+    tc_norm_kernel<<<unsigned((padded + 255) / 256), 256, 0, st>>>(x, rows, int(dim), padded, mc, map, out);
     return cudaGetLastError();
 }
 
@@ -533,7 +620,7 @@ cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_
 
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
-                           cudaStream_t st, int *launches, int *qt_out) {
+                           cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm, const int *rot) {
     // (qt_out receives the query tiles per CTA; segments per split follow from it)
     TcArgs a{};
     a.qt = q_tiles;
@@ -548,14 +635,33 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     a.split_tiles = (a.n_tiles + splits - 1) / splits;
     a.cand = cand;
     a.err = err;
+    a.perm = perm;
+    a.rot = rot;
     int qt = 0, stages = 0;
     if (!tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
+    if ((perm || rot) && qt != 1) return cudaErrorInvalidValue;
     if (qt_out) *qt_out = qt;
     if (launches) *launches += 1;
     const int mc = metric_class(metric);
     if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
     if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
     return launch_tc_mc<1, 2>(a, mc, st);
+}
+
+cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, uint32_t *pivot, int *count,
+                                  int *start, int *cursor, uint32_t *perm, int *rot, cudaStream_t st,
+                                  int *launches) {
+    if (P < 1 || P > 1024 * 64) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(count, 0, size_t(P) * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const unsigned nb = unsigned((n + 255) / 256);
+    nearest_pivot_kernel<<<nb, 256, 0, st>>>(cand, n, segs, pivot, count);
+    bucket_offsets_kernel<<<1, 1024, 0, st>>>(count, P, start, cursor);
+    bucket_scatter_kernel<<<nb, 256, 0, st>>>(pivot, n, cursor, perm);
+    const int64_t qtiles = tc_tiles(n);
+    scan_rotation_kernel<<<unsigned((qtiles + 255) / 256), 256, 0, st>>>(perm, pivot, start, qtiles, rot);
+    if (launches) *launches += 4;
+    return cudaGetLastError();
 }
 
 }  // namespace ssg

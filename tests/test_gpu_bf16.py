@@ -118,6 +118,38 @@ def test_bf16_allknn_exclude_self(ss):
     assert O.macrorecall(gold, gi[rows]) >= 0.99
 
 
+@pytest.mark.parametrize("name", ["normcosine", "sql2", "cosine"])
+def test_bf16_allknn_locality_order_identical(ss, name):
+    # allknn scans a database of >= 32768 rows in its locality order (rows
+    # grouped by nearest pivot, each query tile starting at its own group);
+    # the kept (distance, id) keys do not depend on the order, so the result
+    # equals the id-order scan exactly -- ties between duplicated rows, the
+    # partial last tile and the scan's wrap-around included
+    rng = np.random.default_rng(11 + len(name))
+    n, d = 35007, 96
+    X = mixture(rng, n, d, centres=300, normalise=(name != "sql2"))
+    X[500:700] = X[:200]
+    X[n - 50:] = X[1000:1050]
+    dist = getattr(ss.Dist, NAMES[name])()
+    idx = ss.GPUExhaustiveSearch(dist, ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.25)
+    ids_l, dists_l = ss.allknn(idx, ss.GenericContext(), 16, exclude_self=True)
+    idx.set_param("locality", 0)
+    ids_p, dists_p = ss.allknn(idx, ss.GenericContext(), 16, exclude_self=True)
+    assert np.array_equal(ids_l, ids_p)
+    assert np.array_equal(dists_l, dists_p)
+    idx.set_param("locality", 1)
+    ids_2, _ = ss.allknn(idx, ss.GenericContext(), 16, exclude_self=True)
+    assert np.array_equal(ids_l, ids_2)
+    rows = rng.choice(n, size=200, replace=False)
+    fi, _ = O.searchbatch_f64(name, X, X[rows], 17)
+    gi = np.ascontiguousarray(ids_l.T)[rows]
+    gold = np.zeros((200, 16), dtype=np.uint32)
+    for r, j in enumerate(rows):
+        keep = [t for t in range(17) if fi[r, t] != j + 1][:16]
+        gold[r] = fi[r, keep]
+    assert O.macrorecall(gold, gi) >= 0.98
+
+
 def test_bf16_rejects_hamming(ss):
     # Hamming distances are integers: only the exact method exists for them
     B = np.zeros((10, 2), dtype=np.uint64)
