@@ -83,6 +83,7 @@ struct ssg_index {
     DevBuf loc_perm, loc_rot, loc_tiles, loc_norm;
     int64_t loc_n = -1;
     int locality_param = 1;
+    int wide_param = 1;    // BF16 scan: 256-row database tiles per MMA
     // K-streaming tensor-core path (FP8 mode, and BF16 for dim > 256): operand
     // tiles, per-row FP8 scales, per-row epilogue coefficients, query tiles
     DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
@@ -831,7 +832,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, idx->dim,
                                    kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
                                    static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
-                                   perm, rot),
+                                   perm, rot, idx->wide_param != 0),
                "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
@@ -1645,6 +1646,8 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         if (!idx->graphs_param) clear_graphs(idx);
     } else if (k == "locality") {
         idx->locality_param = value != 0.0;
+    } else if (k == "wide") {
+        idx->wide_param = value != 0.0;
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -1666,6 +1669,7 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "overfetch") *value = idx->overfetch;
     else if (k == "profile") *value = idx->profile;
     else if (k == "locality") *value = idx->locality_param;
+    else if (k == "wide") *value = idx->wide_param;
     else if (k == "graphs") *value = idx->graphs_param;
     else if (k == "graph_replays") *value = double(idx->graph_replays);
     else if (k == "last_graph") *value = idx->last_graph;

@@ -111,7 +111,9 @@ cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t
 cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,
                             cudaStream_t st, int *launches, const uint32_t *map = nullptr);
 // The fused scan: per (query, split) the kk best approximate keys.  *err is
-// set non-zero if a bounded wait gave up.  With perm / rot (allknn over
+// set non-zero if a bounded wait gave up.  wide: 256-row database tiles per
+// MMA when the heaps leave room for its ring (d_tiles then must hold an even
+// number of tiles, as every tile set of the library does).  With perm / rot (allknn over
 // tiles built in a locality order, one launch for all queries): perm[p] is
 // the id of the row at position p of both tile sets, query CTA x starts at
 // database tile rot[x], keys carry ids and each query's candidates go to
@@ -119,7 +121,7 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm = nullptr,
-                           const int *rot = nullptr);
+                           const int *rot = nullptr, bool wide = false);
 // Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
 // segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
 // grouped by pivot) and rot (start tile of each query tile's scan).

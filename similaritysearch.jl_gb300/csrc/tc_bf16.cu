@@ -421,6 +421,276 @@ cudaError_t launch_tc_mc(const TcArgs &a, int mc, cudaStream_t st) {
     return launch_tc_t<QT, STAGES, MC_DOT, FILTER>(a, st);
 }
 
+// ---------------------------------------------------------------------------
+// The wide scan: 256 database rows per MMA (M = 128 queries x N = 256).
+//
+// A 128 x 128 x 16 tcgen05.mma occupies the tensor pipe for 64 cycles, and
+// every MMA and commit adds a fixed cost, so a 128 x 128 tile of 6 MMAs + 2
+// commits runs at ~80% of the pipe's rate even with nothing else on the SM;
+// at N = 256 each MMA is 128 cycles and the commits hide behind it.  The
+// database streams through a ring of K-blocks (256 rows x 32 BF16, the two
+// 128-row tiles' K-blocks side by side: 16 KB), so the heaps still fit next
+// to the ring.  Two accumulators of 128 x 256 FP32 fill all 512 TMEM
+// columns.  Roles, heaps, outputs and the locality order are those of
+// tc_scan_kernel (one query tile per CTA, two epilogue warps per TMEM lane
+// quarter, each owning half of the columns and its own heap).
+// ---------------------------------------------------------------------------
+constexpr int WIDE = 2 * TILE;          // database rows per wide tile
+constexpr int KBLK = TILE * SW;         // bytes of one K-block of a 128-row tile
+
+template <int KST>
+struct WideSmem {
+    static size_t total(int kp, int kk) {
+        return 1024 + size_t(TILE) * kp * 2 + size_t(KST) * 2 * KBLK + TcSmem<1, 1>::heap_bytes(kk) + 256;
+    }
+};
+
+// Heap-mode candidate handling of 32-column chunks (the body of
+// tc_scan_kernel's epilogue for one query row = one lane).
+template <int MC>
+struct ChunkTopK {
+    uint64_t *heap, *cbuf;
+    int hs, kk;
+    int64_t n;
+    const uint32_t *perm;
+    bool qvalid;
+    int nbuf;
+    uint64_t top;
+    float topd, ntopd;
+
+    __device__ __forceinline__ void chunk(const uint32_t (&r)[32], int64_t id0, const float *__restrict__ dnorm) {
+        const float *nrm = dnorm + id0;
+        float dv[32];
+        float gbest[4];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float v = __uint_as_float(r[j]);
+            if (MC == MC_DOT) dv[j] = v;
+            else if (MC == MC_SQ) dv[j] = fmaf(-2.0f, v, __ldg(nrm + j));
+            else dv[j] = -v * __ldg(nrm + j);
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) gbest[g] = MC == MC_DOT ? fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
+        const float cbest = MC == MC_DOT ? fmax3(fmax3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3])
+                                         : fmin3(fmin3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3]);
+        auto passes = [&](float x) { return MC == MC_DOT ? x >= ntopd : x <= topd; };
+        if (!__any_sync(0xffffffffu, passes(cbest))) return;
+        const int lim = int(id0 + 32 <= n ? 32 : n - id0);  // valid columns
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            if (!__any_sync(0xffffffffu, passes(gbest[g]))) continue;
+#pragma unroll
+            for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
+                nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
+            }
+            if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
+                top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, kk, hs, nbuf, top, perm);
+                nbuf = 0;
+                topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                ntopd = -topd;
+            }
+        }
+    }
+};
+
+template <int KST, int MC>
+__global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
+    constexpr int CS = 2;
+    constexpr int NACC = 2;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const size_t tile_bytes = size_t(TILE) * a.kp * 2;  // one 128-row tile (all K-blocks)
+    const int kblocks = a.kp / KBE;
+    uint8_t *sA = smem;
+    uint8_t *sB = sA + tile_bytes;  // KST stages of 2 x KBLK bytes
+    uint64_t *heap_base = reinterpret_cast<uint64_t *>(sB + size_t(KST) * 2 * KBLK);
+    uint64_t *buf_base = heap_base + size_t(TILE) * CS * a.kk;
+    uint64_t *bars = buf_base + size_t(TILE) * CS * kBufCap;
+    uint64_t *a_full = bars;
+    uint64_t *full = bars + 1;
+    uint64_t *empty = full + KST;
+    uint64_t *acc_full = empty + KST;
+    uint64_t *acc_empty = acc_full + NACC;
+    uint64_t *mma_done = acc_empty + NACC;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(a_full, 1);
+        for (int s = 0; s < KST; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < NACC; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], tc_live_warps<1, CS>(a));
+        }
+        tc::mbar_init(mma_done, 1);
+        tc::fence_mbarrier_init();
+    }
+    if (warp == 1) tc::tmem_alloc<512>(tmem_slot);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    // wide tiles (pairs of 128-row tiles: the tile set holds an even count);
+    // split ranges and the locality rotation in wide tiles
+    const int64_t n_wide = (a.n_tiles + 1) / 2;
+    const int64_t split_w = (n_wide + a.splits - 1) / a.splits;
+    const int64_t w_lo = int64_t(blockIdx.y) * split_w;
+    const int64_t w_hi = w_lo + split_w < n_wide ? w_lo + split_w : n_wide;
+    const int W = w_hi > w_lo ? int(w_hi - w_lo) : 0;
+    const int64_t rot = a.rot ? int64_t(a.rot[blockIdx.x]) / 2 : 0;
+    auto phys_wide = [&](int u) {
+        int64_t p = w_lo + u + rot;
+        return p >= n_wide ? p - n_wide : p;
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tc::mbar_arrive_expect_tx(a_full, uint32_t(tile_bytes));
+            tc::bulk_g2s(sA, a.qt + size_t(blockIdx.x) * tile_bytes, uint32_t(tile_bytes), a_full);
+            const int steps = W * kblocks;
+            int issued = 0;
+            for (int st = 0; st < steps; ++st) {
+                const int s = st % KST;
+                if (!tc::mbar_wait(&empty[s], ((st / KST) & 1) ^ 1, a.err, 1)) break;
+                const int u = st / kblocks, kb = st % kblocks;
+                const uint8_t *src = a.dt + size_t(2 * phys_wide(u)) * tile_bytes + size_t(kb) * KBLK;
+                uint8_t *dst = sB + size_t(s) * 2 * KBLK;
+                tc::mbar_arrive_expect_tx(&full[s], uint32_t(2 * KBLK));
+                tc::bulk_g2s(dst, src, uint32_t(KBLK), &full[s]);
+                tc::bulk_g2s(dst + KBLK, src + tile_bytes, uint32_t(KBLK), &full[s]);
+                issued = st + 1;
+            }
+            // wait (bounded) until every copy this thread issued has landed
+            tc::mbar_wait(a_full, 0, a.err, 2);
+            for (int st = issued - KST < 0 ? 0 : issued - KST; st < issued; ++st)
+                tc::mbar_wait(&full[st % KST], (st / KST) & 1, a.err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(TILE, WIDE);
+            bool ok = tc::mbar_wait(a_full, 0, a.err, 3);
+            const uint32_t a_addr = tc::smem_u32(sA);
+            const uint32_t b_addr0 = tc::smem_u32(sB);
+            for (int u = 0; ok && u < W; ++u) {
+                const int b = u & 1;
+                if (!tc::mbar_wait(&acc_empty[b], ((u >> 1) & 1) ^ 1, a.err, 5)) break;
+                const uint32_t d_tmem = tmem_base + uint32_t(b * WIDE);
+                for (int kb = 0; ok && kb < kblocks; ++kb) {
+                    const int st = u * kblocks + kb;
+                    const int s = st % KST;
+                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 4)) { ok = false; break; }
+                    tc::tc_fence_after();
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {  // two K = 16 steps per 32-element K-block
+                        const uint64_t ad = tc::smem_desc(a_addr + uint32_t(kb * KBLK + h * 32), SW);
+                        const uint64_t bd = tc::smem_desc(b_addr0 + uint32_t(s * 2 * KBLK + h * 32), SW);
+                        tc::mma_f16(d_tmem, ad, bd, idesc, (kb > 0 || h > 0) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                tc::mma_commit(&acc_full[b]);
+            }
+            tc::mma_commit(mma_done);
+            tc::mbar_wait(mma_done, 0, a.err, 6);
+        }
+        __syncwarp();
+    } else {
+        const int e = warp - 2;
+        const int cs = e / 4;
+        const int quarter = warp % 4;
+        const int row = quarter * 32 + lane;
+        const int64_t query = int64_t(blockIdx.x) * TILE + row;
+        constexpr int hs = TILE * CS;
+        ChunkTopK<MC> T;
+        T.heap = heap_base + (e * 32 + lane);
+        T.cbuf = buf_base + (e * 32 + lane);
+        T.hs = hs;
+        T.kk = a.kk;
+        T.n = a.n;
+        T.perm = a.perm;
+        T.qvalid = query < a.m;
+        T.nbuf = 0;
+        T.top = KEY_EMPTY;
+        T.topd = T.qvalid ? INFINITY : -INFINITY;
+        T.ntopd = -T.topd;
+        Heap{T.heap, a.kk, hs}.init();
+        const bool warp_live = int64_t(blockIdx.x) * TILE + quarter * 32 < a.m;
+        for (int u = 0; warp_live && u < W; ++u) {
+            const int b = u & 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (u >> 1) & 1, a.err, 7) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            tc::tc_fence_after();
+            // this warp's 128 columns, LDC 32-column loads in flight per
+            // round; the accumulator goes back to the MMA warp as soon as the
+            // last load landed (two accumulators only: the MMAs must not wait
+            // for the filtering).  DOT holds all four chunks in registers;
+            // the norm-scaled metrics need registers for the distances and
+            // take two rounds of two.
+            constexpr int LDC = MC == MC_DOT ? 4 : 2;
+            const int64_t row0 = phys_wide(u) * WIDE + cs * TILE;
+            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * TILE);
+            uint32_t r[LDC][32];
+#pragma unroll
+            for (int round = 0; round < 4 / LDC; ++round) {
+                __syncwarp();
+#pragma unroll
+                for (int c = 0; c < LDC; ++c)
+                    tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
+                tc::tmem_wait_ld();
+                if (round == 4 / LDC - 1) {
+                    tc::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+                }
+#pragma unroll
+                for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+            }
+        }
+        T.top = heap_drain_raw<MC == MC_DOT>(T.heap, T.cbuf, a.kk, hs, T.nbuf, T.top, a.perm);
+        if (query < a.m) {
+            Heap H{T.heap, a.kk, hs};
+            H.sort_ascending();
+            const size_t qrow = a.perm ? size_t(a.perm[query]) : size_t(query);
+            uint64_t *out = a.cand + ((qrow * a.splits + blockIdx.y) * CS + cs) * a.kk;
+            for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc<512>(tmem_base);
+    }
+}
+
+template <int KST, int MC>
+cudaError_t launch_wide_t(const TcArgs &a, cudaStream_t st) {
+    size_t smem = WideSmem<KST>::total(a.kp, a.kk);
+    if (smem < kAloneSmem) smem = kAloneSmem;  // all 512 TMEM columns: alone on the SM
+    auto kern = tc_wide_kernel<KST, MC>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((a.m + TILE - 1) / TILE), unsigned(a.splits));
+    kern<<<grid, tc_threads<1>(), smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int KST>
+cudaError_t launch_wide_mc(const TcArgs &a, int mc, cudaStream_t st) {
+    if (mc == MC_SQ) return launch_wide_t<KST, MC_SQ>(a, st);
+    if (mc == MC_COS) return launch_wide_t<KST, MC_COS>(a, st);
+    return launch_wide_t<KST, MC_DOT>(a, st);
+}
+
 // thr[q] = the smallest over the query's segments of the segment's last
 // (kk-th) key distance: a bound with at least kk sample candidates below it.
 __global__ void sample_bound_kernel(const uint64_t *__restrict__ cand, int64_t m, int segs, int kk,
@@ -544,6 +814,15 @@ int64_t tc_tiles(int64_t rows) { return (rows + TILE - 1) / TILE; }
 size_t tc_tile_bytes(int64_t dim) { return size_t(TILE) * tc_padded_k(dim) * 2; }
 
 // Picks (query tiles per CTA, stages) for this K and candidate count.
+// Ring depth (K-block stages) of the wide scan for this K and candidate
+// count; false if fewer than three stages fit next to the heaps.
+bool wide_choose(int kp, int kk, int *kst) {
+    if (WideSmem<5>::total(kp, kk) <= kMaxSmem) { *kst = 5; return true; }
+    if (WideSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
+    if (WideSmem<3>::total(kp, kk) <= kMaxSmem) { *kst = 3; return true; }
+    return false;
+}
+
 bool tc_choose(int kp, int kk, int *qt, int *stages) {
     // One query tile per CTA with eight epilogue warps measured faster than two
     // query tiles with four warps each (the epilogue, not the database
@@ -620,7 +899,8 @@ cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_
 
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
-                           cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm, const int *rot) {
+                           cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm, const int *rot,
+                           bool wide) {
     // (qt_out receives the query tiles per CTA; segments per split follow from it)
     TcArgs a{};
     a.qt = q_tiles;
@@ -643,6 +923,12 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     if (qt_out) *qt_out = qt;
     if (launches) *launches += 1;
     const int mc = metric_class(metric);
+    int kst = 0;
+    if (wide && wide_choose(a.kp, kk, &kst)) {
+        if (kst == 5) return launch_wide_mc<5>(a, mc, st);
+        if (kst == 4) return launch_wide_mc<4>(a, mc, st);
+        return launch_wide_mc<3>(a, mc, st);
+    }
     if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
     if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
     return launch_tc_mc<1, 2>(a, mc, st);
