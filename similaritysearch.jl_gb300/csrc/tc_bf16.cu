@@ -16,7 +16,14 @@
 // copy (cp.async.bulk) of a tile lands in shared memory ready for the MMA --
 // no tensor map and no reformatting on chip.
 //
-// CTA roles (QT query tiles of 128 rows each, 64 + 128*QT threads):
+// Two scans share this layout: tc_wide_kernel (heap mode, 128 x 256 MMAs
+// over a ring of database K-blocks; the default) and tc_scan_kernel (128 x
+// 128 tiles: the threshold filter, and candidate counts whose heaps leave no
+// room for the wide ring).  allknn may scan the database in a locality order
+// (rows grouped by nearest pivot; see launch_locality_order).
+//
+// tc_scan_kernel's CTA roles (QT query tiles of 128 rows each, 64 + 128*QT
+// threads):
 //   warp 0      TMA producer: the QT query tiles once, then database tiles
 //               through a STAGES-deep ring;
 //   warp 1      owns TMEM (2 x QT accumulators of 128 x 128 FP32) and issues
