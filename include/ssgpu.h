@@ -150,7 +150,10 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * the direct difference-form scan only), "plain" (1 = plain FP32 method on a
  * BF16/FP8 index, e.g. to calibrate "overfetch" against it), "profile"
  * (1 = time the scan kernel with events), "graphs" (0 = no CUDA-graph replay
- * in ssg_search_batches).  Unknown keys return SSG_EINVAL. */
+ * in ssg_search_batches), "wide" (0 = BF16 scans in 128 x 128 tiles instead
+ * of 128 x 256), "locality" (0 = BF16 allknn scans in id order instead of
+ * the pivot-grouped order; results are identical either way).  Unknown keys
+ * return SSG_EINVAL. */
 int ssg_set_param(ssg_index *idx, const char *key, double value);
 /* Readable keys: the tunables plus "n", "dim", "metric", "precision",
  * "main_kernel_ms" / "main_kernel_launches" (accumulated while profiling),
