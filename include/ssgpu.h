@@ -111,15 +111,14 @@ int ssg_search_device(ssg_index *idx, const void *dev_q, int64_t m, int32_t k,
 /* Runs nb query batches of different sizes and k as one search: batch b has
  * m[b] queries at dev_q[b] (device rows of dim elements of the index's type)
  * and receives m[b] rows of k[b] results at dev_ids[b] / dev_dists[b] (device
- * memory).  The arrays themselves are host arrays of nb entries.  All batches
- * share the query tiles and one scan of the database with the candidates of
- * the largest k; batch b's rows are the first k[b] entries of that search
- * (for the plain method exactly the rows of a separate call; for BF16/FP8 a
- * candidate list at least as long).  Batches with m[b] == 0 are skipped.
- * Replaces per-request searchbatch! calls on a request stream.  With the
- * reduced-precision scans the device work of a call is replayed from a CUDA
- * graph when its shape (queries rounded up to 32, largest k) repeats
- * ("graphs" param, default 1; "graph_replays", "last_graph" readable). */
+ * memory).  The arrays themselves are host arrays of nb entries.  Batches of
+ * the same k share the query tiles and one scan of the database (one scan per
+ * distinct k), so each batch's rows are those of a separate call with its k.
+ * Batches with m[b] == 0 are skipped.  Replaces per-request searchbatch!
+ * calls on a request stream.  With the reduced-precision scans the device
+ * work of each k's search is replayed from a CUDA graph when its shape
+ * (queries rounded up to 32, k) repeats ("graphs" param, default 1;
+ * "graph_replays", "last_graph" readable). */
 int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, const int64_t *m,
                        const int32_t *k, uint32_t *const *dev_ids, float *const *dev_dists);
 

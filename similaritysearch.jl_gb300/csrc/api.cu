@@ -1241,7 +1241,7 @@ std::vector<uint64_t> graph_key(const ssg_index *idx, int64_t m, int k) {
     static_assert(sizeof(double) == 8, "double");
     memcpy(&of, &idx->overfetch, 8);
     std::vector<uint64_t> key = {uint64_t(m), uint64_t(k), uint64_t(idx->n), uint64_t(idx->prec),
-                                 uint64_t(idx->metric), of, uint64_t(idx->splits_param)};
+                                 uint64_t(idx->metric), of, uint64_t(idx->splits_param), uint64_t(idx->wide_param)};
     for (const DevBuf *b : {&idx->db, &idx->db_norm, &idx->tc_db, &idx->tc_norm, &idx->tc_q, &idx->st_db,
                             &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale, &idx->cand,
                             &idx->red[0], &idx->red[1], &idx->status, &idx->gbound, &idx->qnorm, &idx->pack_q,
@@ -1510,55 +1510,66 @@ int ssg_search_batches(ssg_index *idx, int32_t nb, const void *const *dev_q, con
     if (nb <= 0 || !dev_q || !m || !k || !dev_ids || !dev_dists)
         return fail(idx, SSG_EINVAL, "need nb > 0 batches and non-NULL arrays");
     int64_t mt = 0;
-    int32_t kmax = 0;
+    // batches grouped by k: each group is one packed search with its own
+    // candidate count, so a k = 1 batch never pays for a k = 100 batch's heaps
+    std::map<int32_t, std::vector<int32_t>> groups;
     for (int32_t b = 0; b < nb; ++b) {
         if (m[b] < 0 || k[b] <= 0) return fail(idx, SSG_EINVAL, "batch %d: m must be >= 0 and k > 0", b);
         if (m[b] > 0 && (!dev_q[b] || !dev_ids[b] || !dev_dists[b]))
             return fail(idx, SSG_EINVAL, "batch %d: NULL query or output pointer", b);
         mt += m[b];
-        if (m[b] > 0) kmax = std::max(kmax, k[b]);
+        if (m[b] > 0) groups[k[b]].push_back(b);
     }
     if (mt == 0) return SSG_OK;
     if (idx->n == 0) return fail(idx, SSG_EINVAL, "the index is empty");
-    // pack the batches' queries (one copy each), one search with the largest
-    // k, then each batch's first k columns back to its own output.  Graph
-    // replays need a fixed shape: the packed count is rounded up to a
-    // multiple of 32 zero rows (the granularity of the small-batch heaps, so
-    // a small window keeps the small-batch kernel configuration).
-    const bool graph = idx->elem == SSG_ELEM_F32 && graph_capturable(idx, kmax);
-    const int64_t mrun = graph ? (mt + 31) / 32 * 32 : mt;
     const size_t row_bytes = size_t(idx->dim) * elem_size(idx->elem);
-    SSG_CK(idx->pack_q.ensure(size_t(mrun) * row_bytes), "allocating packed queries");
-    SSG_CK(idx->pack_out.ensure(size_t(mrun) * kmax * 8), "allocating packed results");
-    char *pq = static_cast<char *>(idx->pack_q.p);
-    int64_t off = 0;
-    for (int32_t b = 0; b < nb; ++b) {
-        if (m[b] == 0) continue;
-        SSG_CK(cudaMemcpyAsync(pq + size_t(off) * row_bytes, dev_q[b], size_t(m[b]) * row_bytes,
-                               cudaMemcpyDeviceToDevice, idx->stream),
-               "packing queries");
-        off += m[b];
-    }
-    if (mrun > mt)
-        SSG_CK(cudaMemsetAsync(pq + size_t(mt) * row_bytes, 0, size_t(mrun - mt) * row_bytes, idx->stream),
-               "padding packed queries");
-    uint32_t *pi = static_cast<uint32_t *>(idx->pack_out.p);
-    float *pd = reinterpret_cast<float *>(pi + size_t(mrun) * kmax);
     idx->last_graph = 0;
-    int rc = graph ? search_graph(idx, pq, mrun, kmax, pi, pd) : search_locked(idx, pq, mt, kmax, pi, pd, true);
-    if (rc) return rc;
-    off = 0;
-    for (int32_t b = 0; b < nb; ++b) {
-        if (m[b] == 0) continue;
-        SSG_CK(cudaMemcpy2DAsync(dev_ids[b], size_t(k[b]) * 4, pi + size_t(off) * kmax, size_t(kmax) * 4,
-                                 size_t(std::min(k[b], kmax)) * 4, size_t(m[b]), cudaMemcpyDeviceToDevice,
-                                 idx->stream),
-               "unpacking ids");
-        SSG_CK(cudaMemcpy2DAsync(dev_dists[b], size_t(k[b]) * 4, pd + size_t(off) * kmax, size_t(kmax) * 4,
-                                 size_t(std::min(k[b], kmax)) * 4, size_t(m[b]), cudaMemcpyDeviceToDevice,
-                                 idx->stream),
-               "unpacking distances");
-        off += m[b];
+    for (const auto &grp : groups) {
+        const int32_t kg = grp.first;
+        int64_t mg = 0;
+        for (int32_t b : grp.second) mg += m[b];
+        // pack the group's queries (one copy each), one search, then each
+        // batch's rows back to its own output.  Graph replays need a fixed
+        // shape: the packed count is rounded up to a multiple of 32 zero rows
+        // (the granularity of the small-batch heaps, so a small window keeps
+        // the small-batch kernel configuration).
+        const bool graph = idx->elem == SSG_ELEM_F32 && graph_capturable(idx, kg);
+        const int64_t mrun = graph ? (mg + 31) / 32 * 32 : mg;
+        SSG_CK(idx->pack_q.ensure(size_t(mrun) * row_bytes), "allocating packed queries");
+        SSG_CK(idx->pack_out.ensure(size_t(mrun) * kg * 8), "allocating packed results");
+        char *pq = static_cast<char *>(idx->pack_q.p);
+        int64_t off = 0;
+        for (int32_t b : grp.second) {
+            SSG_CK(cudaMemcpyAsync(pq + size_t(off) * row_bytes, dev_q[b], size_t(m[b]) * row_bytes,
+                                   cudaMemcpyDeviceToDevice, idx->stream),
+                   "packing queries");
+            off += m[b];
+        }
+        // padding rows repeat the group's first query: a zero query would tie
+        // every database row at distance 0 under IP / NormCosine, and then its
+        // heaps take every column as a candidate (slow, though still correct)
+        for (int64_t done = 0; done < mrun - mg;) {
+            const int64_t c = done == 0 ? 1 : std::min(done, mrun - mg - done);
+            const char *src = done == 0 ? pq : pq + size_t(mg) * row_bytes;
+            SSG_CK(cudaMemcpyAsync(pq + size_t(mg + done) * row_bytes, src, size_t(c) * row_bytes,
+                                   cudaMemcpyDeviceToDevice, idx->stream),
+                   "padding packed queries");
+            done += c;
+        }
+        uint32_t *pi = static_cast<uint32_t *>(idx->pack_out.p);
+        float *pd = reinterpret_cast<float *>(pi + size_t(mrun) * kg);
+        const int rc = graph ? search_graph(idx, pq, mrun, kg, pi, pd) : search_locked(idx, pq, mg, kg, pi, pd, true);
+        if (rc) return rc;
+        off = 0;
+        for (int32_t b : grp.second) {
+            SSG_CK(cudaMemcpyAsync(dev_ids[b], pi + size_t(off) * kg, size_t(m[b]) * kg * 4,
+                                   cudaMemcpyDeviceToDevice, idx->stream),
+                   "unpacking ids");
+            SSG_CK(cudaMemcpyAsync(dev_dists[b], pd + size_t(off) * kg, size_t(m[b]) * kg * 4,
+                                   cudaMemcpyDeviceToDevice, idx->stream),
+                   "unpacking distances");
+            off += m[b];
+        }
     }
     return finish_call(idx, true);
 }

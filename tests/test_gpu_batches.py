@@ -1,5 +1,6 @@
 """GPU tests of ssg_search_batches: uneven batches with mixed k answered by
-one search, and the CUDA-graph replay of its device work."""
+one packed search per distinct k, and the CUDA-graph replay of its device
+work."""
 import numpy as np
 import pytest
 
@@ -90,6 +91,30 @@ def test_batches_graph_replay(ss, precision, d, name, ks, overfetch):
             assert all(np.float32(O.evaluate(name, X[i - 1], q[j])) == np.float32(dd) for dd, i in pairs)
         fi, _ = O.searchbatch_f64(name, X, q, k)
         assert O.macrorecall(fi, gi) >= 0.99
+
+
+@pytest.mark.parametrize("precision,d,name,overfetch", [("fp8", 384, "ip", 4.0), ("bf16", 96, "sql2", 2.0)])
+def test_batches_reduced_precision_equal_separate_calls(ss, precision, d, name, overfetch):
+    # batches of one k share a packed search; a query's kept candidates do not
+    # depend on the other queries of its search (padding rows, splits and the
+    # shared pruning bounds leave the kept key set unchanged), so every batch
+    # gets exactly the rows of a separate call with its own k -- also when its
+    # search is replayed from a graph
+    rng = np.random.default_rng(d + 1)
+    sizes = [3, 64, 0, 17, 200, 1, 40]
+    ks = [10, 1, 10, 100, 10, 1, 100]
+    X, Q = data(rng, 20000, d, sum(sizes))
+    dist = ss.Dist.SqL2() if name == "sql2" else ss.Dist.InnerProduct()
+    idx = ss.GPUExhaustiveSearch(dist, ss.MatrixDatabase.from_rows(X), precision=precision, overfetch=overfetch)
+    ctx = ss.GenericContext(logger=None)
+    runs = [ss.searchbatches(idx, ctx, dbs(ss, split(Q, sizes)), ks) for _ in range(3)]
+    for res in runs:
+        for (ids, dists), q, k in zip(res, split(Q, sizes), ks):
+            assert ids.shape == (k, q.shape[0])
+            if q.shape[0] == 0:
+                continue
+            ri, rd = ss.searchbatch(idx, ctx, ss.MatrixDatabase.from_rows(q), k)
+            assert np.array_equal(ids, ri) and np.array_equal(dists, rd)
 
 
 def test_batches_argument_errors(ss):
