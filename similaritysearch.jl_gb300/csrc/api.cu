@@ -50,7 +50,6 @@ struct DevBuf {
     }
 };
 
-bool is_float_metric(int m) { return m >= SSG_METRIC_SQL2 && m <= SSG_METRIC_IP; }
 bool is_sq_metric(int metric) { return metric == SSG_METRIC_SQL2 || metric == SSG_METRIC_L2; }
 
 size_t elem_size(int e) {
@@ -526,7 +525,6 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
 
 int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k, int exclude_self,
              uint32_t *d_ids, float *d_dists, int kk) {
-    const int take = k + (exclude_self ? 1 : 0);
     const bool sq = is_sq_metric(idx->metric);
     const int64_t qtiles = (m + 127) / 128;
     int64_t splits = idx->splits_param > 0

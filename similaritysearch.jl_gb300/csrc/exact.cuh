@@ -25,14 +25,15 @@ __device__ __forceinline__ float exact_pair(const void *dbv, int64_t row, int64_
     const float *x = static_cast<const float *>(dbv) + row * dim;
     const float *q = static_cast<const float *>(qv) + j * dim;
     float acc = 0.0f;
-    if (METRIC == SQL2 || METRIC == L2) {
+    if constexpr (METRIC == SQL2 || METRIC == L2) {
         for (int64_t c = 0; c < dim; ++c) { float m = x[c] - q[c]; acc = fmaf(m, m, acc); }
         return METRIC == L2 ? sqrtf(acc) : acc;
+    } else {
+        for (int64_t c = 0; c < dim; ++c) acc = fmaf(x[c], q[c], acc);
+        if (METRIC == NORMCOSINE) return 1.0f - acc;
+        if (METRIC == IP) return -acc;
+        return 1.0f - acc / (xn[row] * qn[j]);
     }
-    for (int64_t c = 0; c < dim; ++c) acc = fmaf(x[c], q[c], acc);
-    if (METRIC == NORMCOSINE) return 1.0f - acc;
-    if (METRIC == IP) return -acc;
-    return 1.0f - acc / (xn[row] * qn[j]);
 }
 
 }  // namespace ssg

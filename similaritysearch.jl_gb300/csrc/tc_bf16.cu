@@ -56,7 +56,6 @@ enum { MC_DOT = 0, MC_SQ = 1, MC_COS = 2 };
 // every 8 columns with a trigger of 4, so at most 3 + 8 entries are pending.
 constexpr int kBufCap = 12;
 constexpr int kDrainTrigger = 4;
-constexpr int kDrainEvery = 8;
 
 // Column splits of the epilogue: with one query tile per CTA, two warps share
 // each TMEM lane quarter and filter half of the tile's columns each (two heaps

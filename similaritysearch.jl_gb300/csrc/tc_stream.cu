@@ -39,7 +39,6 @@ constexpr int SWB = 128;                      // bytes per swizzled K-block row
 constexpr int KBLOCK_BYTES = TILE * SWB;      // 16 KB per operand per K-block
 constexpr int kBufCap = 12;
 constexpr int kDrainTrigger = 4;
-constexpr int kDrainEvery = 8;
 // TMEM accumulators (128 columns each): all 512 columns, so the MMAs run up
 // to three tiles ahead of the epilogue
 constexpr int NACC = 4;
