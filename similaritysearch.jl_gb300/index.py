@@ -157,6 +157,38 @@ class GPUExhaustiveSearch:
         self.set_param("overfetch", chosen)
         return chosen
 
+    def autotune_scan(self, Q, k: int, repeats: int = 3,
+                      splits=(0, 1, 2, 4, 8, 16, 32, 64), widths=(1, 0)) -> dict:
+        """Picks the scan shape for searches like ``searchbatch(self, ctx, Q,
+        k)`` by timing them: the database tile width of the BF16 scan
+        ("wide": 128 x 256 or 128 x 128 MMA tiles) and the database splits
+        per query tile ("splits", 0 = the wave model).  Every shape keeps the
+        same candidates, so only the time changes; the fastest (median of
+        ``repeats`` calls after a warm-up) is set and returned with the
+        timings.  A no-op for the plain method."""
+        import time
+        if self.precision == "fp32":
+            return {}
+        ctx = GenericContext(logger=None)
+        widths = widths if self.precision == "bf16" else (int(self.get_param("wide")),)
+        timings = {}
+        for w in widths:
+            self.set_param("wide", w)
+            for s in splits:
+                self.set_param("splits", s)
+                searchbatch(self, ctx, Q, k)
+                ts = []
+                for _ in range(max(1, repeats)):
+                    t0 = time.perf_counter()
+                    searchbatch(self, ctx, Q, k)
+                    ts.append(time.perf_counter() - t0)
+                timings[(w, s)] = sorted(ts)[len(ts) // 2]
+        best = min(timings, key=timings.get)
+        self.set_param("wide", best[0])
+        self.set_param("splits", best[1])
+        return {"wide": best[0], "splits": best[1], "seconds": timings[best],
+                "timings": {f"wide={w},splits={s}": t for (w, s), t in timings.items()}}
+
     def train_mlp(self, sample: int = 50_000, triplets: int = 200_000, epochs: int = 4, hidden: int = 256,
                   out_dim: int = 64, batch: int = 1024, lr: float = 1e-3, seed: int = 1,
                   target_recall: float | None = None) -> dict:

@@ -150,6 +150,32 @@ def test_bf16_allknn_locality_order_identical(ss, name):
     assert O.macrorecall(gold, gi) >= 0.98
 
 
+def test_bf16_autotune_scan_keeps_results(ss):
+    # the autotuner times scan shapes (tile width, database splits); every
+    # shape keeps the same candidates, so the tuned index answers exactly as
+    # the default one
+    rng = np.random.default_rng(21)
+    X = mixture(rng, 20000, 96)
+    Q = X[rng.integers(0, 20000, size=300)] + rng.standard_normal((300, 96), dtype=np.float32) * 0.02
+    Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.NormCosine(), ss.MatrixDatabase.from_rows(X), precision="bf16",
+                                 overfetch=2.0)
+    ctx = ss.GenericContext()
+    qdb = ss.MatrixDatabase.from_rows(Q)
+    ids0, d0 = ss.searchbatch(idx, ctx, qdb, 10)
+    tuned = idx.autotune_scan(qdb, 10, repeats=1, splits=(0, 1, 4, 16))
+    assert tuned["wide"] in (0, 1) and tuned["splits"] in (0, 1, 4, 16)
+    assert len(tuned["timings"]) == 8
+    assert idx.get_param("wide") == tuned["wide"] and idx.get_param("splits") == tuned["splits"]
+    ids1, d1 = ss.searchbatch(idx, ctx, qdb, 10)
+    assert np.array_equal(ids0, ids1) and np.array_equal(d0, d1)
+    for w, sp in ((0, 1), (1, 16), (0, 16)):
+        idx.set_param("wide", w)
+        idx.set_param("splits", sp)
+        ids2, d2 = ss.searchbatch(idx, ctx, qdb, 10)
+        assert np.array_equal(ids0, ids2) and np.array_equal(d0, d2)
+
+
 def test_bf16_rejects_hamming(ss):
     # Hamming distances are integers: only the exact method exists for them
     B = np.zeros((10, 2), dtype=np.uint64)
