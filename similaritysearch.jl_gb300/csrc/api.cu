@@ -781,11 +781,12 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     int kk = int(kk64);
     int qt = 0, stages = 0;
     idx->last_fallbacks = 0;
-    // more candidates than the kernel's on-chip heaps hold: threshold filter
-    if (!ssg::tc_choose(kp, kk, &qt, &stages))
+    // more candidates than the scans' on-chip heaps hold: threshold filter
+    // (the wide scan, one query tile per CTA, is chosen first when it fits)
+    const bool wide = idx->wide_param && ssg::tc_wide_fits(kp, kk);
+    if (wide) qt = 1;
+    else if (!ssg::tc_choose(kp, kk, &qt, &stages))
         return run_knn_tc_filter(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db, kk);
-    if (!ssg::tc_choose(kp, kk, &qt, &stages))
-        return fail(idx, SSG_EUNSUPPORTED, "k = %d does not fit the BF16 kernel's on-chip top-k", take);
     const int64_t qrows = int64_t(qt) * 128;
     const int64_t qctas = (m + qrows - 1) / qrows;
     const int64_t n_tiles = ssg::tc_tiles(idx->n);
@@ -961,7 +962,8 @@ int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t 
         } else {
             SSG_CK(ssg::launch_tc_scan(idx->metric, qc_tiles, static_cast<const uint8_t *>(idx->tc_smp.p),
                                        static_cast<const float *>(idx->tc_smp_norm.p), idx->smp_rows, mc, idx->dim,
-                                       kSampleK, 1, cand, status, idx->stream, &idx->last_launches, nullptr),
+                                       kSampleK, 1, cand, status, idx->stream, &idx->last_launches, nullptr,
+                                       nullptr, nullptr, true),
                    "launching the sample scan");
             SSG_CK(ssg::launch_sample_bound(cand, mc, segs_s, kSampleK, thr, idx->stream, &idx->last_launches),
                    "computing filter bounds");
@@ -1229,7 +1231,8 @@ bool graph_capturable(ssg_index *idx, int k) {
         return false;
     if (uses_stream(idx)) return true;
     int qt = 0, stages = 0;
-    return ssg::tc_choose(ssg::tc_padded_k(idx->dim), int(overfetch_kk(idx, k)), &qt, &stages);
+    const int kp = ssg::tc_padded_k(idx->dim), kk = int(overfetch_kk(idx, k));
+    return (idx->wide_param && ssg::tc_wide_fits(kp, kk)) || ssg::tc_choose(kp, kk, &qt, &stages);
 }
 
 // Everything a captured graph depends on: shape, method, tunables and the

@@ -100,6 +100,8 @@ int64_t tc_tiles(int64_t rows);
 size_t tc_tile_bytes(int64_t dim);
 // Chooses query tiles per CTA and pipeline depth; false if kk cannot fit.
 bool tc_choose(int kp, int kk, int *qt, int *stages);
+// Whether the wide scan's heaps and ring fit for this K and candidate count.
+bool tc_wide_fits(int kp, int kk);
 // Sorted candidate segments the scan writes per (query, split) for a CTA with
 // `qt` query tiles (the epilogue splits a tile's columns between warps).
 int tc_segments_per_split(int qt);

@@ -822,6 +822,11 @@ size_t tc_tile_bytes(int64_t dim) { return size_t(TILE) * tc_padded_k(dim) * 2; 
 // Picks (query tiles per CTA, stages) for this K and candidate count.
 // Ring depth (K-block stages) of the wide scan for this K and candidate
 // count; false if fewer than three stages fit next to the heaps.
+bool wide_choose(int kp, int kk, int *kst);
+bool tc_wide_fits(int kp, int kk) {
+    int kst = 0;
+    return wide_choose(kp, kk, &kst);
+}
 bool wide_choose(int kp, int kk, int *kst) {
     if (WideSmem<5>::total(kp, kk) <= kMaxSmem) { *kst = 5; return true; }
     if (WideSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
@@ -878,9 +883,19 @@ cudaError_t launch_tc_filter(int metric, const uint8_t *q_tiles, const uint8_t *
     a.fout = fout;
     a.fcount = fcount;
     a.fcap = fcap;
-    if (TcSmem<1, 4>::total(a.kp, 0) > kMaxSmem) return cudaErrorInvalidValue;
+    // four ring stages, fewer for wide K (at K = 256 two fit)
+    const int mc = metric_class(metric);
+    if (TcSmem<1, 4>::total(a.kp, 0) <= kMaxSmem) {
+        if (launches) *launches += 1;
+        return launch_tc_mc<1, 4, true>(a, mc, st);
+    }
+    if (TcSmem<1, 3>::total(a.kp, 0) <= kMaxSmem) {
+        if (launches) *launches += 1;
+        return launch_tc_mc<1, 3, true>(a, mc, st);
+    }
+    if (TcSmem<1, 2>::total(a.kp, 0) > kMaxSmem) return cudaErrorInvalidValue;
     if (launches) *launches += 1;
-    return launch_tc_mc<1, 4, true>(a, metric_class(metric), st);
+    return launch_tc_mc<1, 2, true>(a, mc, st);
 }
 
 cudaError_t launch_sample_bound(const uint64_t *cand, int64_t m, int segs, int kk, float *thr, cudaStream_t st,
@@ -923,14 +938,14 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     a.err = err;
     a.perm = perm;
     a.rot = rot;
-    int qt = 0, stages = 0;
-    if (!tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
+    int qt = 1, stages = 0, kst = 0;
+    const bool use_wide = wide && wide_choose(a.kp, kk, &kst);
+    if (!use_wide && !tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
     if ((perm || rot) && qt != 1) return cudaErrorInvalidValue;
     if (qt_out) *qt_out = qt;
     if (launches) *launches += 1;
     const int mc = metric_class(metric);
-    int kst = 0;
-    if (wide && wide_choose(a.kp, kk, &kst)) {
+    if (use_wide) {
         if (kst == 5) return launch_wide_mc<5>(a, mc, st);
         if (kst == 4) return launch_wide_mc<4>(a, mc, st);
         return launch_wide_mc<3>(a, mc, st);

@@ -150,6 +150,28 @@ def test_bf16_allknn_locality_order_identical(ss, name):
     assert O.macrorecall(gold, gi) >= 0.98
 
 
+@pytest.mark.parametrize("d,k,name", [(96, 50, "normcosine"), (256, 10, "sql2"), (32, 1, "ip"), (200, 20, "cosine")])
+def test_bf16_wide_equals_narrow(ss, d, k, name):
+    # the wide scan (128 x 256 MMAs, K-block ring; at d = 96, k = 50 its
+    # heaps leave room for three stages only, at d = 256 eight K-blocks per
+    # tile) keeps exactly the candidates of the 128 x 128 scan; at d >= 200
+    # the 128 x 128 scan's ring does not fit beside the heaps and the
+    # threshold filter answers instead, with the same candidates unless it
+    # falls back to the exact scan
+    rng = np.random.default_rng(d + k)
+    X = mixture(rng, 9000, d, normalise=(name != "sql2" and name != "ip"))
+    Q = X[rng.integers(0, 9000, size=260)] + rng.standard_normal((260, d), dtype=np.float32) * 0.02
+    if name == "normcosine":
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    gi, gd = run(ss, name, X, Q, k, overfetch=1.25, wide=1)
+    ni, nd = run(ss, name, X, Q, k, overfetch=1.25, wide=0)
+    if d < 200:
+        assert np.array_equal(gi, ni) and np.array_equal(gd, nd)
+    check_reported_distances_exact(name, X, Q, gi[:10], gd[:10])
+    fi, _ = O.searchbatch_f64(name, X, Q, k)
+    assert O.macrorecall(fi, gi) >= 0.97
+
+
 def test_bf16_autotune_scan_keeps_results(ss):
     # the autotuner times scan shapes (tile width, database splits); every
     # shape keeps the same candidates, so the tuned index answers exactly as
@@ -184,13 +206,14 @@ def test_bf16_rejects_hamming(ss):
 
 
 @pytest.mark.parametrize("name", ["sql2", "cosine", "ip"])
-@pytest.mark.parametrize("n,k", [(30000, 200), (6000, 300)])
-def test_bf16_large_k_threshold_filter(ss, name, n, k):
+@pytest.mark.parametrize("n,k,d", [(30000, 200, 64), (6000, 300, 64), (20000, 150, 256)])
+def test_bf16_large_k_threshold_filter(ss, name, n, k, d):
     # k beyond the on-chip heaps: the sampled-bound filter path (n > 8192) or
-    # the every-row path (n <= 8192), then the exact rerank
+    # the every-row path (n <= 8192), then the exact rerank; at d = 256 the
+    # filter scan runs with two ring stages and the sample scan wide
     rng = np.random.default_rng(n + k + len(name))
-    X = mixture(rng, n, 64, normalise=False)
-    Q = X[rng.integers(0, n, size=150)] + rng.standard_normal((150, 64), dtype=np.float32) * 0.05
+    X = mixture(rng, n, d, normalise=False)
+    Q = X[rng.integers(0, n, size=150)] + rng.standard_normal((150, d), dtype=np.float32) * 0.05
     gi, gd = run(ss, name, X, Q, k, overfetch=1.5)
     check_reported_distances_exact(name, X, Q[:10], gi[:10], gd[:10])
     fi, _ = O.searchbatch_f64(name, X, Q, k)
