@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
                     if (__any_sync(0xffffffffu, passes(cbest))) {
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
-                            if (passes(dv[j]) && id0 + j < a.n) {
+                            if (passes(dv[j]) && id0 + j < a.n && qvalid) {
                                 const float d = MC == MC_DOT ? -dv[j] : dv[j];
                                 const int pos = atomicAdd(a.fcount + query, 1);
                                 if (pos < a.fcap) a.fout[size_t(query) * a.fcap + pos] = make_key(d, uint32_t(id0 + j));
