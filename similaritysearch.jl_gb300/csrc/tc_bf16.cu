@@ -178,6 +178,78 @@ __device__ __forceinline__ int tc_live_warps(const TcArgs &a) {
     return live;
 }
 
+// The scans' candidate handling of one 32-column chunk for one query row
+// (one lane): the approximate distance of each column and the best per group
+// of 8 columns, a warp vote on the chunk and on each group, then
+//   heap mode: branch-free raw appends (the slot is always written with the
+//     column's id and value, the count only advances for a candidate; the
+//     key is made when the buffer drains into the lane's heap);
+//   FILTER: every column at or below the query's fixed bound appended to
+//     its list of fcap keys (fcount counts them all; rare, ~3 kk of n).
+// DOT ranks by -v: its columns keep v, take the maximum and compare with
+// -topd (exact: negation is exact).
+template <int MC, bool FILTER = false>
+struct ChunkTopK {
+    uint64_t *heap, *cbuf;
+    int hs, kk;
+    int64_t n;
+    const uint32_t *perm;
+    bool qvalid;
+    int nbuf;
+    uint64_t top;
+    float topd, ntopd;
+    uint64_t *fout;  // FILTER: lists of fcap keys per query, counts
+    int *fcount;
+    int fcap;
+    int64_t query;
+
+    __device__ __forceinline__ void chunk(const uint32_t (&r)[32], int64_t id0, const float *__restrict__ dnorm) {
+        const float *nrm = dnorm + id0;
+        float dv[32];
+        float gbest[4];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float v = __uint_as_float(r[j]);
+            if (MC == MC_DOT) dv[j] = v;
+            else if (MC == MC_SQ) dv[j] = fmaf(-2.0f, v, __ldg(nrm + j));
+            else dv[j] = -v * __ldg(nrm + j);
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) gbest[g] = MC == MC_DOT ? fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
+        const float cbest = MC == MC_DOT ? fmax3(fmax3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3])
+                                         : fmin3(fmin3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3]);
+        auto passes = [&](float x) { return MC == MC_DOT ? x >= ntopd : x <= topd; };
+        if (!__any_sync(0xffffffffu, passes(cbest))) return;
+        const int lim = int(id0 + 32 <= n ? 32 : n - id0);  // valid columns
+        if constexpr (FILTER) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (passes(dv[j]) && j < lim && qvalid) {
+                    const int pos = atomicAdd(fcount + query, 1);
+                    if (pos < fcap)
+                        fout[size_t(query) * fcap + pos] = make_key(MC == MC_DOT ? -dv[j] : dv[j], uint32_t(id0 + j));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                if (!__any_sync(0xffffffffu, passes(gbest[g]))) continue;
+#pragma unroll
+                for (int j = 8 * g; j < 8 * g + 8; ++j) {
+                    cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
+                    nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
+                }
+                if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
+                    top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, kk, hs, nbuf, top, perm);
+                    nbuf = 0;
+                    topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
+                    ntopd = -topd;
+                }
+            }
+        }
+    }
+};
+
 template <int QT, int STAGES, int MC, bool FILTER>
 __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) {
     constexpr int CS = col_splits<QT>();
@@ -298,18 +370,27 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         const int64_t query = (int64_t(blockIdx.x) * QT + q) * TILE + row;
         constexpr int hs = QT * TILE * CS;
         constexpr int CHUNKS = TILE / 32 / CS;  // 32-column chunks per warp and tile
-        uint64_t *heap = heap_base + (e * 32 + lane);
-        uint64_t *cbuf = buf_base + (e * 32 + lane);
-        if (!FILTER) Heap{heap, a.kk, hs}.init();
         // padding rows of a partial query tile filter everything out (a
         // -inf threshold), and warps holding only padding rows skip the
         // epilogue: they just hand the accumulator back
-        const bool qvalid = query < a.m;
+        ChunkTopK<MC, FILTER> T;
+        T.heap = heap_base + (e * 32 + lane);
+        T.cbuf = buf_base + (e * 32 + lane);
+        T.hs = hs;
+        T.kk = a.kk;
+        T.n = a.n;
+        T.perm = a.perm;
+        T.qvalid = query < a.m;
+        T.nbuf = 0;
+        T.top = KEY_EMPTY;
+        T.topd = T.qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
+        T.ntopd = -T.topd;
+        T.fout = a.fout;
+        T.fcount = a.fcount;
+        T.fcap = a.fcap;
+        T.query = query;
+        if (!FILTER) Heap{T.heap, a.kk, hs}.init();
         const bool warp_live = (int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
-        uint64_t top = KEY_EMPTY;
-        float topd = qvalid ? (FILTER ? a.thr[query] : INFINITY) : -INFINITY;
-        float ntopd = -topd;
-        int nbuf = 0;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
             const int b = t % NACC;
             int ok = 1;
@@ -331,67 +412,10 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
 #pragma unroll
-            for (int c = 0; c < CHUNKS; ++c) {
-                const int64_t id0 = row0 + c * 32;
-                const float *nrm = a.dnorm + id0;
-                // approximate distance of each column and the best per group
-                // of 8 columns.  DOT ranks by -v: its columns keep v, take the
-                // maximum and compare with -topd (exact: negation is exact)
-                float dv[32];
-                float gbest[4];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float v = __uint_as_float(r[c][j]);
-                    if (MC == MC_DOT) dv[j] = v;
-                    else if (MC == MC_SQ) dv[j] = fmaf(-2.0f, v, __ldg(nrm + j));
-                    else dv[j] = -v * __ldg(nrm + j);
-                }
-#pragma unroll
-                for (int g = 0; g < 4; ++g) gbest[g] = MC == MC_DOT ? fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
-                const float cbest = MC == MC_DOT ? fmax3(fmax3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3])
-                                                 : fmin3(fmin3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3]);
-                // x is at or below the query's bound
-                auto passes = [&](float x) { return MC == MC_DOT ? x >= ntopd : x <= topd; };
-                if (FILTER) {
-                    // rare: ~3 * kk of the n columns pass a query's threshold
-                    if (__any_sync(0xffffffffu, passes(cbest))) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            if (passes(dv[j]) && id0 + j < a.n && qvalid) {
-                                const float d = MC == MC_DOT ? -dv[j] : dv[j];
-                                const int pos = atomicAdd(a.fcount + query, 1);
-                                if (pos < a.fcap) a.fout[size_t(query) * a.fcap + pos] = make_key(d, uint32_t(id0 + j));
-                            }
-                        }
-                    }
-                    continue;
-                }
-                if (__any_sync(0xffffffffu, passes(cbest))) {
-                    const int lim = int(id0 + 32 <= a.n ? 32 : a.n - id0);  // valid columns
-#pragma unroll
-                    for (int g = 0; g < 4; ++g) {
-                        if (!__any_sync(0xffffffffu, passes(gbest[g]))) continue;
-#pragma unroll
-                        for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                            // branch-free raw append: the slot is always
-                            // written (the id and the column's value; the key
-                            // is made when the buffer drains), the count only
-                            // advances for a candidate
-                            cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
-                            nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
-                        }
-                        if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
-                            top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top, a.perm);
-                            nbuf = 0;
-                            topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                            ntopd = -topd;
-                        }
-                    }
-                }
-            }
+            for (int c = 0; c < CHUNKS; ++c) T.chunk(r[c], row0 + c * 32, a.dnorm);
         }
-        if (!FILTER) top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, a.kk, hs, nbuf, top, a.perm);
-        Heap H{heap, a.kk, hs};
+        if (!FILTER) T.top = heap_drain_raw<MC == MC_DOT>(T.heap, T.cbuf, a.kk, hs, T.nbuf, T.top, a.perm);
+        Heap H{T.heap, a.kk, hs};
         if (!FILTER && query < a.m) {
             H.sort_ascending();
             // the candidates of a query go to its row by id
@@ -448,55 +472,6 @@ template <int KST>
 struct WideSmem {
     static size_t total(int kp, int kk) {
         return 1024 + size_t(TILE) * kp * 2 + size_t(KST) * 2 * KBLK + TcSmem<1, 1>::heap_bytes(kk) + 256;
-    }
-};
-
-// Heap-mode candidate handling of 32-column chunks (the body of
-// tc_scan_kernel's epilogue for one query row = one lane).
-template <int MC>
-struct ChunkTopK {
-    uint64_t *heap, *cbuf;
-    int hs, kk;
-    int64_t n;
-    const uint32_t *perm;
-    bool qvalid;
-    int nbuf;
-    uint64_t top;
-    float topd, ntopd;
-
-    __device__ __forceinline__ void chunk(const uint32_t (&r)[32], int64_t id0, const float *__restrict__ dnorm) {
-        const float *nrm = dnorm + id0;
-        float dv[32];
-        float gbest[4];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const float v = __uint_as_float(r[j]);
-            if (MC == MC_DOT) dv[j] = v;
-            else if (MC == MC_SQ) dv[j] = fmaf(-2.0f, v, __ldg(nrm + j));
-            else dv[j] = -v * __ldg(nrm + j);
-        }
-#pragma unroll
-        for (int g = 0; g < 4; ++g) gbest[g] = MC == MC_DOT ? fmax8(dv + 8 * g) : fmin8(dv + 8 * g);
-        const float cbest = MC == MC_DOT ? fmax3(fmax3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3])
-                                         : fmin3(fmin3(gbest[0], gbest[1], gbest[2]), gbest[3], gbest[3]);
-        auto passes = [&](float x) { return MC == MC_DOT ? x >= ntopd : x <= topd; };
-        if (!__any_sync(0xffffffffu, passes(cbest))) return;
-        const int lim = int(id0 + 32 <= n ? 32 : n - id0);  // valid columns
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-            if (!__any_sync(0xffffffffu, passes(gbest[g]))) continue;
-#pragma unroll
-            for (int j = 8 * g; j < 8 * g + 8; ++j) {
-                cbuf[nbuf * hs] = (uint64_t(uint32_t(id0) + uint32_t(j)) << 32) | __float_as_uint(dv[j]);
-                nbuf += (passes(dv[j]) && j < lim) ? 1 : 0;
-            }
-            if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
-                top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, kk, hs, nbuf, top, perm);
-                nbuf = 0;
-                topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                ntopd = -topd;
-            }
-        }
     }
 };
 
@@ -626,6 +601,10 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
         T.top = KEY_EMPTY;
         T.topd = T.qvalid ? INFINITY : -INFINITY;
         T.ntopd = -T.topd;
+        T.fout = nullptr;
+        T.fcount = nullptr;
+        T.fcap = 0;
+        T.query = query;
         Heap{T.heap, a.kk, hs}.init();
         const bool warp_live = int64_t(blockIdx.x) * TILE + quarter * 32 < a.m;
         for (int u = 0; warp_live && u < W; ++u) {
