@@ -18,21 +18,23 @@
 //
 // Two scans share this layout: tc_wide_kernel (heap mode, 128 x 256 MMAs
 // over a ring of database K-blocks; the default) and tc_scan_kernel (128 x
-// 128 tiles: the threshold filter, and candidate counts whose heaps leave no
-// room for the wide ring).  allknn may scan the database in a locality order
+// 128 tiles: the threshold filter, the "wide" = 0 setting and the locality
+// order's pivot scan).  allknn may scan the database in a locality order
 // (rows grouped by nearest pivot; see launch_locality_order).
 //
-// tc_scan_kernel's CTA roles (QT query tiles of 128 rows each, 64 + 128*QT
-// threads):
-//   warp 0      TMA producer: the QT query tiles once, then database tiles
-//               through a STAGES-deep ring;
-//   warp 1      owns TMEM (2 x QT accumulators of 128 x 128 FP32) and issues
-//               the MMAs from one thread; accumulators are double-buffered so
-//               the epilogue of tile t overlaps the MMAs of tile t+1;
-//   warps 2..   epilogue: thread = one query row = one TMEM lane; reads its
-//               row 32 columns at a time (tcgen05.ld 32x32b.x32), filters
-//               against its heap frontier, and keeps its own top-kk heap in
-//               shared memory.
+// CTA roles (one 128-row query tile, 320 threads):
+//   warp 0      TMA producer: the query tile once, then database tiles (or
+//               K-blocks of two tiles) through a ring;
+//   warp 1      owns TMEM (four 128 x 128 FP32 accumulators, two 128 x 256
+//               in the wide scan, two 128 x 128 for the filter) and issues
+//               the MMAs from one thread; the accumulators rotate so the
+//               epilogue of one tile overlaps the MMAs of the next;
+//   warps 2..9  epilogue, two warps per TMEM lane quarter, each with half of
+//               a tile's columns: thread = one query row = one TMEM lane;
+//               reads its row 32 columns at a time (tcgen05.ld 32x32b.x32),
+//               filters against its heap frontier (or the filter's bound)
+//               and keeps its own top-kk heap in shared memory
+//               (ChunkTopK).
 // Every mbarrier wait is bounded (tc_ptx.cuh); a timeout sets *err and all
 // roles unwind, wait for their own in-flight copies/MMAs, free TMEM and exit.
 #include "common.cuh"
