@@ -31,9 +31,16 @@ namespace {
 
 thread_local char g_err[512] = "";
 
+// A device allocation owned by one object: freed by release() or when the
+// object goes out of scope (temporaries of a call free their memory on every
+// return path), never copied.
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
     cudaError_t ensure(size_t want) {
         if (want <= bytes) return cudaSuccess;
         if (p) cudaFree(p);
