@@ -257,8 +257,15 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
         if (rc) { cudaFree(S); err = "sample index creation failed"; learned_free(m); return rc; }
         uint32_t *nn_ids = nullptr;
         float *nn_d = nullptr;
-        cudaMalloc(&nn_ids, size_t(ns) * 10 * 4);
-        cudaMalloc(&nn_d, size_t(ns) * 10 * 4);
+        if (cudaMalloc(&nn_ids, size_t(ns) * 10 * 4) != cudaSuccess || cudaMalloc(&nn_d, size_t(ns) * 10 * 4) != cudaSuccess) {
+            cudaGetLastError();
+            if (nn_ids) cudaFree(nn_ids);
+            ssg_destroy(tmp);
+            cudaFree(S);
+            err = "allocating the sample's neighbours";
+            learned_free(m);
+            return SSG_ENOMEM;
+        }
         rc = ssg_allknn_device(tmp, 10, 1, nn_ids, nn_d);
         std::vector<uint32_t> nn(size_t(ns) * 10);
         if (!rc) cudaMemcpy(nn.data(), nn_ids, nn.size() * 4, cudaMemcpyDeviceToHost);
@@ -293,6 +300,8 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
         float *mom = dmalloc(2 * npar, cu, "adam");
         float *stat = dmalloc(2, cu, "loss");
         if (!X || !Hh || !Z || !dZ || !dH || !gW1 || !gb1 || !gW2 || !gb2 || !mom || !stat) {
+            for (float *p : {X, Hh, Z, dZ, dH, gW1, gb1, gW2, gb2, mom, stat})
+                if (p) cudaFree(p);
             cudaFree(S); cudaFree(d_trip);
             return fail(SSG_ENOMEM);
         }
