@@ -19,10 +19,13 @@ Arms:
                      reference cannot run on this machine), timed on a bounded
                      sample of the same workload
 
-Other workloads of the benchmark suite (`--workload c1|c3`) print a line of
-the same shape: C1 searchbatch SqL2 (d=128, n=100,000, m=1,000, k=10) and C3
-Hamming (2,000,000 sketches of 1,024 bits, 10,000 queries at 10 % bit flips,
-k=100).
+Other workloads of the benchmark suite (`--workload c1|c3|c4|c5`) print a
+line of the same shape: C1 searchbatch SqL2 (d=128, n=100,000, m=1,000,
+k=10); C3 Hamming (2,000,000 sketches of 1,024 bits, 10,000 queries at 10 %
+bit flips, k=100); C4 a request stream of 200 uneven batches (1-4096
+queries, k in {1, 10, 100}) over 2,000,000 vectors of d=768 in FP8 with the
+exact rerank, per call and coalesced; C5 the learned shortlist on the C4
+database.
 
 The timed device region has the database resident in HBM (the C2 database is
 384 MB FP32, larger than the 129 MB L2, so no flush is needed between steps).
