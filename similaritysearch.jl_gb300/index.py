@@ -171,18 +171,25 @@ class GPUExhaustiveSearch:
             return {}
         ctx = GenericContext(logger=None)
         widths = widths if self.precision == "bf16" else (int(self.get_param("wide")),)
+        before = (int(self.get_param("wide")), int(self.get_param("splits")))
         timings = {}
-        for w in widths:
-            self.set_param("wide", w)
-            for s in splits:
-                self.set_param("splits", s)
-                searchbatch(self, ctx, Q, k)
-                ts = []
-                for _ in range(max(1, repeats)):
-                    t0 = time.perf_counter()
+        try:
+            for w in widths:
+                self.set_param("wide", w)
+                for s in splits:
+                    self.set_param("splits", s)
                     searchbatch(self, ctx, Q, k)
-                    ts.append(time.perf_counter() - t0)
-                timings[(w, s)] = sorted(ts)[len(ts) // 2]
+                    ts = []
+                    for _ in range(max(1, repeats)):
+                        t0 = time.perf_counter()
+                        searchbatch(self, ctx, Q, k)
+                        ts.append(time.perf_counter() - t0)
+                    timings[(w, s)] = sorted(ts)[len(ts) // 2]
+        except BaseException:
+            # a failed trial leaves the index as it was
+            self.set_param("wide", before[0])
+            self.set_param("splits", before[1])
+            raise
         best = min(timings, key=timings.get)
         self.set_param("wide", best[0])
         self.set_param("splits", best[1])
