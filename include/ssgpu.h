@@ -249,12 +249,17 @@ int ssg_bitsketch(const void *dev_R, int64_t dim, int64_t outdim, const void *de
  * SQL2, L2, NORMCOSINE, IP, HAMMING (COSINE returns SSG_EUNSUPPORTED).
  * Results are those of ssg_search_device on the same data in the plain
  * method.  The candidate scratch is a fixed 16 MiB array inside the library:
- * m * min(k, n) must not exceed 2,097,152 (SSG_EINVAL otherwise).  The first
- * call on a device looks up that array's address, so make it before any
- * stream capture.  The work is enqueued on `stream` (a cudaStream_t, NULL =
- * default stream) and the call returns without waiting for it.  All calls
- * share the array: calls that overlap on the GPU race, calls ordered on one
- * stream do not. */
+ * m * min(k, n) must not exceed 2,097,152 (SSG_EINVAL otherwise).  The array
+ * is reserved on a device by the first call into this library there (the
+ * module loads lazily), so a caller whose pool will take the whole GPU should
+ * make one small call first.  Each uncaptured call looks up the array's
+ * device address; a captured call reuses the one found by the last uncaptured
+ * call on the device, so make the first call before any stream capture.
+ * Buffers must be aligned to their element (8 bytes for sketches, 4 for the
+ * rest; SSG_EINVAL otherwise).  The work is enqueued on `stream` (a
+ * cudaStream_t, NULL = default stream) and the call returns without waiting
+ * for it.  All calls share the array: calls that overlap on the GPU race,
+ * calls ordered on one stream do not. */
 int ssg_knn_noalloc(int metric, const void *dev_db, int64_t dim, int64_t n,
                     const void *dev_q, int64_t m, int32_t k,
                     uint32_t *dev_ids, float *dev_dists, void *stream);

@@ -9,7 +9,8 @@
 //
 // Block = QPB threads, one query per thread; the query's words live in
 // registers (zero-padded to WMAX words).  Database sketches stream through
-// shared memory in tiles of TN rows and are read with 128-bit broadcast loads;
+// shared memory in tiles of TN rows, copied 16 bytes at a time (cp.async;
+// 8 bytes for odd word counts) and read with 128-bit broadcast loads;
 // every thread XORs + popcounts them against its own query and pushes the
 // distance into its private max-heap when it beats the frontier.
 #include "common.cuh"
@@ -34,20 +35,38 @@ __device__ __forceinline__ void cp_async8(uint64_t *dst, const uint64_t *src, bo
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(valid ? 8 : 0) : "memory");
 }
 
-// tile of TN sketches starting at row j0 (rows >= hi and words >= W are zeros)
-template <int WMAX, int QPB>
+// 16-byte asynchronous copy global -> shared (L2 only), zero-filled when !valid
+__device__ __forceinline__ void cp_async16(uint64_t *dst, const uint64_t *src, bool valid) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+// tile of TN sketches starting at row j0 (rows >= hi and words >= W are
+// zeros).  VEC16: two words per copy, for an even W on a 16-byte aligned
+// database (every word pair then starts on a 16-byte boundary).
+template <int WMAX, int QPB, bool VEC16>
 __device__ __forceinline__ void load_sketches(uint64_t (*xs)[WMAX], const uint64_t *__restrict__ db, int64_t j0,
                                               int64_t hi, int W) {
-    for (int e = threadIdx.x; e < TN * WMAX; e += QPB) {
-        const int r = e / WMAX, c = e % WMAX;
-        const int64_t xr = j0 + r;
-        const bool v = xr < hi && c < W;
-        cp_async8(&xs[r][c], v ? db + xr * W + c : db, v);
+    if constexpr (VEC16) {
+        for (int e = threadIdx.x; e < TN * WMAX / 2; e += QPB) {
+            const int r = e / (WMAX / 2), c = 2 * (e % (WMAX / 2));
+            const int64_t xr = j0 + r;
+            const bool v = xr < hi && c < W;
+            cp_async16(&xs[r][c], v ? db + xr * W + c : db, v);
+        }
+    } else {
+        for (int e = threadIdx.x; e < TN * WMAX; e += QPB) {
+            const int r = e / WMAX, c = e % WMAX;
+            const int64_t xr = j0 + r;
+            const bool v = xr < hi && c < W;
+            cp_async8(&xs[r][c], v ? db + xr * W + c : db, v);
+        }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-template <int WMAX, int QPB>
+template <int WMAX, int QPB, bool VEC16>
 __global__ void __launch_bounds__(QPB)
 hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__restrict__ Q,
                int heap_in_smem) {
@@ -71,11 +90,11 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
     BufferedTopK T;
     T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
 
-    if (lo < hi) load_sketches<WMAX, QPB>(xbuf, db, lo, hi, W);
+    if (lo < hi) load_sketches<WMAX, QPB, VEC16>(xbuf, db, lo, hi, W);
     for (int64_t j0 = lo, it = 0; j0 < hi; j0 += TN, ++it) {
         // the next tile lands while this one is scanned
         if (j0 + TN < hi) {
-            load_sketches<WMAX, QPB>(xbuf + ((it + 1) & 1) * TN, db, j0 + TN, hi, W);
+            load_sketches<WMAX, QPB, VEC16>(xbuf + ((it + 1) & 1) * TN, db, j0 + TN, hi, W);
             asm volatile("cp.async.wait_group 1;" ::: "memory");
         } else {
             asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -139,7 +158,10 @@ template <int WMAX, int QPB>
 cudaError_t launch_ham_t(const ScanArgs &a, const uint64_t *db, const uint64_t *q, cudaStream_t st) {
     const bool in_smem = ham_heap_fits<WMAX, QPB>(a.kk);
     size_t smem = ham_static_smem<WMAX, QPB>() + (in_smem ? size_t(a.kk + kBufCap) * QPB * 8 : 0);
-    auto kern = hamming_kernel<WMAX, QPB>;
+    // 16-byte copies need every word pair 16-byte aligned: an even W and an
+    // aligned base (the library's own buffers are; caller buffers may not be)
+    const bool vec16 = (a.dim % 2 == 0) && (reinterpret_cast<uintptr_t>(db) % 16 == 0);
+    auto kern = vec16 ? hamming_kernel<WMAX, QPB, true> : hamming_kernel<WMAX, QPB, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + QPB - 1) / QPB), unsigned(a.splits));

@@ -12,15 +12,21 @@
 //
 // The array.  g_noalloc_keys is a file-scope __device__ array of
 // kNoAllocKeys 64-bit keys (16 MiB).  Every GPU that loads the library holds
-// it until the process exits.  Host code cannot use the array's name as a
-// device address (on the host it only names a stand-in), so the first call on
-// each device resolves the real address with cudaGetSymbolAddress while that
-// device is current and caches it; that first call should therefore come
-// before any stream capture.  Nothing in the array has to start at zero: the
-// scan writes every key slot the merge later reads.  All calls share the one
-// array and leave the last call's keys in it, so calls whose work overlaps on
-// the GPU (different streams, or several host threads without ordering) race;
-// calls issued in order on one stream do not.
+// it until the process exits.  With lazy module loading (the CUDA default) the
+// array is reserved by the first call into this library on a device, whatever
+// that call is: a caller whose own pool will reserve the whole GPU should make
+// one small call first (an m = 1 search, say) so that the reservation happens
+// before its pool takes the memory.  Host code cannot use the array's name as
+// a device address (on the host it only names a stand-in), so each call
+// resolves the real address with cudaGetSymbolAddress while the device is
+// current.  The lookup allocates nothing once the module is loaded; during a
+// stream capture the address cached by an earlier call on the device is used
+// instead (a capture must not load modules), so the first call on a device
+// should come before any stream capture.  Nothing in the array has to start
+// at zero: the scan writes every key slot the merge later reads.  All calls
+// share the one array and leave the last call's keys in it, so calls whose
+// work overlaps on the GPU (different streams, or several host threads
+// without ordering) race; calls issued in order on one stream do not.
 #include "ssgpu.h"
 #include "common.cuh"
 #include "kernels.h"
@@ -45,14 +51,23 @@ int fail(int code, const char *fmt, long long a = 0, long long b = 0) {
     return ssg::report_error(code, buf);
 }
 
-// Device address of g_noalloc_keys on the current device (set up once).
-int keys_for_current_device(uint64_t **out) {
+// Device address of g_noalloc_keys on the current device.  Outside a stream
+// capture it is looked up on every call (so a device reset, which unloads
+// the module, never leaves a stale address behind); while `st` is capturing
+// the address cached by the last uncaptured call on this device is used.
+int keys_for_current_device(cudaStream_t st, uint64_t **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SSG_ECUDA, "no current CUDA device");
     if (dev < 0 || dev >= kMaxDevices) return fail(SSG_EUNSUPPORTED, "device ordinal %lld out of range", dev);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SSG_ECUDA, "querying the stream's capture status failed");
+    }
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_keys_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_keys);
         if (e != cudaSuccess || !p) {
@@ -60,10 +75,15 @@ int keys_for_current_device(uint64_t **out) {
             return fail(SSG_ECUDA, "resolving the scratch array's device address failed");
         }
         g_keys_addr[dev] = p;
+    } else if (!g_keys_addr[dev]) {
+        return fail(SSG_EINVAL, "the first no-allocation search on a device must not be captured: "
+                                "make one call before capturing");
     }
     *out = static_cast<uint64_t *>(g_keys_addr[dev]);
     return SSG_OK;
 }
+
+bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
 }  // namespace
 
@@ -74,6 +94,13 @@ extern "C" int ssg_knn_noalloc(int metric, const void *dev_db, int64_t dim, int6
                                       "Hamming (Cosine needs per-row norms, i.e. more scratch)");
     if (metric < SSG_METRIC_SQL2 || metric > SSG_METRIC_HAMMING) return fail(SSG_EUNSUPPORTED, "unknown metric %lld", metric);
     if (!dev_db || !dev_q || !dev_ids || !dev_dists) return fail(SSG_EINVAL, "NULL device pointer");
+    // the scans read Float32 rows element by element and sketches word by
+    // word: misaligned buffers are refused here instead of faulting on the GPU
+    const uintptr_t row_align = metric == SSG_METRIC_HAMMING ? 8 : 4;
+    if (!aligned(dev_db, row_align) || !aligned(dev_q, row_align))
+        return fail(SSG_EINVAL, "database and query buffers must be %lld-byte aligned", (long long)row_align);
+    if (!aligned(dev_ids, 4) || !aligned(dev_dists, 4))
+        return fail(SSG_EINVAL, "result buffers must be 4-byte aligned");
     if (dim <= 0 || n <= 0 || m <= 0 || k <= 0)
         return fail(SSG_EINVAL, "dim, n, m and k must be positive");
     if (metric == SSG_METRIC_HAMMING && dim > 32)
@@ -108,12 +135,12 @@ extern "C" int ssg_knn_noalloc(int metric, const void *dev_db, int64_t dim, int6
         return fail(SSG_EUNSUPPORTED, "k = %lld needs more top-k storage than shared memory holds "
                                       "(the no-allocation search keeps its heaps on chip)", k);
 
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint64_t *keys = nullptr;
-    int rc = keys_for_current_device(&keys);
+    int rc = keys_for_current_device(st, &keys);
     if (rc) return rc;
     a.cand = keys;
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     if (metric == SSG_METRIC_HAMMING)
         e = ssg::launch_hamming(a, static_cast<const uint64_t *>(dev_db), static_cast<const uint64_t *>(dev_q), st,

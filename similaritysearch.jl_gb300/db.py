@@ -99,6 +99,38 @@ class VectorDatabase(AbstractDatabase):
             self.push_item(v)
 
 
+class SubDatabase(AbstractDatabase):
+    """Read-only view of ``parent`` objects ``map[1], map[2], ...`` (1-based
+    ids), src/db/subdatabase.jl: what SearchGraph construction hands to
+    ExhaustiveSearch for its gold standards (query samples, reference sets).
+    Uploaded to the GPU as the gathered rows."""
+
+    def __init__(self, parent, ids):
+        self.parent = parent
+        self.map = np.asarray(ids, dtype=np.int64).reshape(-1)
+        if self.map.size and (self.map.min() < 1 or self.map.max() > len(parent)):
+            raise IndexError("SubDatabase ids out of range")
+
+    def __len__(self):
+        return int(self.map.size)
+
+    @property
+    def dim(self):
+        return self.parent.dim
+
+    @property
+    def dtype(self):
+        return self.parent.dtype
+
+    def __getitem__(self, i: int):
+        if not 1 <= i <= len(self):
+            raise IndexError(i)
+        return self.parent[int(self.map[i - 1])]
+
+    def rows(self) -> np.ndarray:
+        return np.ascontiguousarray(self.parent.rows()[self.map - 1])
+
+
 # MMapMatrixDatabase files (src/db/mmapmatrixdatabase.jl:10-27): a 4096-byte
 # header -- magic UInt64 @0, version Int32 @8, dim Int64 @12, element type
 # code Int32 @20, length n Int64 @24 -- then the column-major (dim, capacity)

@@ -25,7 +25,7 @@ from . import _native as N
 from .db import AbstractDatabase, MatrixDatabase, MMapMatrixDatabase, VectorDatabase, as_database
 from .dist import PreMetric
 from .log import LOG, InformativeLog
-from .pqueue import AbstractKnnQueue, KnnSorted
+from .pqueue import AbstractKnnQueue, AbstractMetricQueue, KnnSorted
 
 ArgumentError = N.ArgumentError
 
@@ -258,10 +258,16 @@ def _col_major_view(a: np.ndarray):
     return np.asfortranarray(a), True
 
 
-def searchbatch_b(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, ids: np.ndarray, dists: np.ndarray,
+def searchbatch_b(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, ids, dists: np.ndarray | None = None,
                   sorted: bool = False):
     """searchbatch!(index, ctx, Q, ids, dists; sorted) -- src/SimilaritySearch.jl:331-348.
-    Columns come back sorted by (distance, id) whether or not ``sorted``."""
+    Columns come back sorted by (distance, id) whether or not ``sorted``.
+
+    searchbatch!(index, ctx, Q, knns) -- src/SimilaritySearch.jl:384-398:
+    with a sequence of per-query queues in place of ``ids`` (and no
+    ``dists``), query j's results are pushed into ``knns[j]``."""
+    if dists is None and not isinstance(ids, np.ndarray):
+        return _searchbatch_queues(idx, ctx, Q, ids)
     rows = idx._queries(Q)
     m = rows.shape[0]
     if m <= 0:
@@ -278,6 +284,35 @@ def searchbatch_b(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, ids: np.ndar
         dists[...] = od
     add_distance_evaluations(ctx, len(idx) * m)
     return ids, dists
+
+
+def _searchbatch_queues(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, knns):
+    """The queue-vector searchbatch!: one GPU search with the largest k of the
+    queues, then each KnnSorted queue receives its query's first maxlength()
+    results in (distance, id) order -- the state the reference's pushes of
+    every object would leave, since a queue of k keeps exactly the first k of
+    that order (also when it already held items).  Radius queues and other
+    containers raise ArgumentError: the GPU index answers fixed-k queries
+    only, and does not fall back to another method."""
+    knns = list(knns)
+    m = len(as_database(Q))
+    if m <= 0:
+        raise ArgumentError("empty set of queries")
+    if m != len(knns):
+        raise ArgumentError("the number of queries is different from the given output containers")
+    for res in knns:
+        if not isinstance(res, AbstractMetricQueue):
+            raise ArgumentError(f"{type(res).__name__} is not a result queue")
+        if not isinstance(res, KnnSorted):
+            raise ArgumentError(f"the GPU index fills KnnSorted queues only, not {type(res).__name__}")
+    k = max(res.maxlength() for res in knns)
+    ids, dists = searchbatch(idx, ctx, Q, k)
+    for j, res in enumerate(knns):
+        for i in range(res.maxlength()):
+            if ids[i, j] == 0:
+                break
+            res.push_item(int(ids[i, j]), float(dists[i, j]))
+    return knns
 
 
 def searchbatch(idx: GPUExhaustiveSearch, ctx: GenericContext, Q, k: int, sorted: bool = True):

@@ -19,8 +19,41 @@ class IdDist:
     dist: float
 
 
-class AbstractKnnQueue:
-    pass
+class AbstractMetricQueue:
+    """Any per-query result container (src/pqueue/pqueue.jl)."""
+
+
+class AbstractKnnQueue(AbstractMetricQueue):
+    """Fixed-k containers (KnnSorted, KnnHeap)."""
+
+
+class AbstractRadiusQueue(AbstractMetricQueue):
+    """Radius-bounded, growable containers (RadiusSorted, RadiusHeap)."""
+
+
+class RadiusSorted(AbstractRadiusQueue):
+    """Every (id, dist) with dist <= radius, kept sorted by distance
+    (src/pqueue/radiussorted.jl:28-52).  A host container: the GPU index
+    answers fixed-k queries only and rejects it."""
+
+    def __init__(self, radius: float):
+        self.radius = np.float32(radius)
+        self.ids: list[int] = []
+        self.dists: list[float] = []
+
+    def __len__(self):
+        return len(self.ids)
+
+    def push_item(self, i: int, dist: float) -> bool:
+        dist = np.float32(dist)
+        if dist > self.radius:
+            return False
+        pos = len(self.dists)
+        while pos > 0 and self.dists[pos - 1] > dist:
+            pos -= 1
+        self.ids.insert(pos, int(i))
+        self.dists.insert(pos, float(dist))
+        return True
 
 
 class KnnSorted(AbstractKnnQueue):

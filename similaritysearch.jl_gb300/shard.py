@@ -7,8 +7,9 @@ per-rank top-k lists are merged by the ``(distance, id)`` key -- what
 to (src/exact/parallel-exhaustive.jl:64-102, src/pqueue/knnsorted.jl:140-168).
 
 The exchange is one ``all_gather`` of ``m x k`` ids and distances per rank
-(8 B per entry), over whatever process group the caller initialised (NCCL on
-GPUs, gloo on CPU).  Replicas -- independent ranks answering independent
+(8 B per entry), over whatever process group the caller initialised: on an
+NCCL group the lists travel as tensors on the rank's current GPU, on gloo as
+host tensors.  Replicas -- independent ranks answering independent
 query streams -- need only ``max_over_ranks`` for timing.
 """
 from __future__ import annotations
@@ -58,13 +59,18 @@ def sharded_searchbatch(local_search, Q, k: int, n: int, group=None):
     li, ld = local_search(Q, k)
     li = np.asarray(li, dtype=np.uint32)
     gi = np.where(li != 0, li + np.uint32(lo), 0).astype(np.uint32)
+    # NCCL moves device tensors only: gather on this rank's GPU there, on the
+    # host for gloo
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend(group) == "nccl" else None
     ti = torch.from_numpy(gi.astype(np.int64))
     td = torch.from_numpy(np.asarray(ld, dtype=np.float32).copy())
+    if dev is not None:
+        ti, td = ti.to(dev), td.to(dev)
     all_i = [torch.empty_like(ti) for _ in range(world)]
     all_d = [torch.empty_like(td) for _ in range(world)]
     dist.all_gather(all_i, ti, group=group)
     dist.all_gather(all_d, td, group=group)
-    return merge_topk([t.numpy().astype(np.uint32) for t in all_i], [t.numpy() for t in all_d], k)
+    return merge_topk([t.cpu().numpy().astype(np.uint32) for t in all_i], [t.cpu().numpy() for t in all_d], k)
 
 
 def max_over_ranks(value: float, group=None, device=None) -> float:

@@ -109,3 +109,37 @@ def test_host_evaluate_known_values(ss, case):
         expect = np.float32(case["expect"])
     tol = 0.0 if m == "hamming" else max(float(case.get("atol", 0.0)), 1e-5 * max(1.0, abs(float(expect))))
     assert abs(float(got) - float(expect)) <= tol
+
+
+def test_queue_vector_searchbatch_rejects_radius_queues_before_searching(ss):
+    """searchbatch!(index, ctx, Q, knns) with a radius queue raises
+    ArgumentError (src/SimilaritySearch.jl:384-398 accepts any
+    AbstractMetricQueue; the GPU index answers fixed-k queries only and never
+    falls back to another method).  Checked before any search runs, so an
+    index object that would fail if touched stands in for the GPU index."""
+    import pytest
+    from similaritysearch_gb300.index import _searchbatch_queues
+
+    class Untouchable:
+        def __getattr__(self, name):
+            raise AssertionError("the index must not be used")
+
+    Q = ss.MatrixDatabase.from_rows(np.zeros((3, 4), dtype=np.float32))
+    ctx = ss.GenericContext(logger=None)
+    queues = [ss.KnnSorted(k=5), ss.RadiusSorted(0.3), ss.KnnSorted(k=2)]
+    with pytest.raises(ss.ArgumentError, match="KnnSorted"):
+        _searchbatch_queues(Untouchable(), ctx, Q, queues)
+    with pytest.raises(ss.ArgumentError, match="number of queries"):
+        _searchbatch_queues(Untouchable(), ctx, Q, [ss.KnnSorted(k=5)])
+    with pytest.raises(ss.ArgumentError, match="not a result queue"):
+        _searchbatch_queues(Untouchable(), ctx, Q, [ss.KnnSorted(k=5), None, ss.KnnSorted(k=1)])
+
+
+def test_radius_sorted_mirror_keeps_items_within_radius_sorted(ss):
+    """RadiusSorted (src/pqueue/radiussorted.jl:28-52): accepts dist <= radius,
+    keeps ascending order, later equal distances after earlier ones."""
+    r = ss.RadiusSorted(0.5)
+    for i, d in [(1, 0.4), (2, 0.6), (3, 0.1), (4, 0.4), (5, 0.5)]:
+        r.push_item(i, d)
+    assert r.ids == [3, 1, 4, 5]
+    assert r.dists == [np.float32(0.1), np.float32(0.4), np.float32(0.4), np.float32(0.5)]

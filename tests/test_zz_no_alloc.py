@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from conftest import load_package
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -80,6 +81,10 @@ def test_noalloc_equals_search_device_twice(env, metric_name):
         gi, gd = noalloc_search(ss, torch, metric, dX, dQ, 40, X.shape[0], Q.shape[0], k)
         assert np.array_equal(gi, ri)
         assert np.array_equal(gd, rd)
+        # and directly against the oracle's sequential (lanes=1) restatement
+        oi, od = O.searchbatch(metric_name.lower(), X, Q, k, lanes=1)
+        assert np.array_equal(gi, oi)
+        assert np.array_equal(gd, od)
 
 
 def test_noalloc_hamming_twice(env):
@@ -111,3 +116,42 @@ def test_noalloc_rejects_requests_beyond_the_fixed_scratch(env):
     rc = N.lib().ssg_knn_noalloc(N.METRIC_COSINE, C.c_void_p(dX.data_ptr()), 8, 3000, C.c_void_p(dQ.data_ptr()),
                                  10, 5, C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()), None)
     assert rc == N.SSG_EUNSUPPORTED
+
+
+def test_noalloc_scratch_caps_the_splits(env):
+    """m * min(k, n) just below the 2,097,152-key scratch: the database would
+    be split four ways to fill the GPU, but only one split's keys fit, so the
+    scan runs unsplit; results still equal ssg_search_device's, twice."""
+    ss, torch = env
+    N = ss._native
+    rng = np.random.default_rng(33)
+    n, m, k, d = 200_000, 20_000, 100, 16
+    X = rng.standard_normal((n, d), dtype=np.float32)
+    Q = rng.standard_normal((m, d), dtype=np.float32)
+    assert m * k <= 2_097_152 < 2 * m * k
+    ri, rd = reference_search(ss, torch, N.METRIC_SQL2, N.ELEM_F32, X, Q, k)
+    dX = torch.from_numpy(X).cuda()
+    dQ = torch.from_numpy(Q).cuda()
+    for _ in range(2):
+        gi, gd = noalloc_search(ss, torch, N.METRIC_SQL2, dX, dQ, d, n, m, k)
+        assert np.array_equal(gi, ri)
+        assert np.array_equal(gd, rd)
+
+
+def test_noalloc_refuses_misaligned_buffers(env):
+    """Buffers not aligned to their element are refused on the host (no
+    kernel runs), instead of faulting on the GPU."""
+    ss, torch = env
+    N = ss._native
+    L = N.lib()
+    dX = torch.zeros((1024, 8), dtype=torch.int64, device="cuda")
+    dQ = torch.zeros((4, 8), dtype=torch.int64, device="cuda")
+    ids = torch.empty((4, 5), dtype=torch.int32, device="cuda")
+    dists = torch.empty((4, 5), dtype=torch.float32, device="cuda")
+    p = lambda t, off=0: C.c_void_p(t.data_ptr() + off)
+    rc = L.ssg_knn_noalloc(N.METRIC_HAMMING, p(dX, 4), 8, 1000, p(dQ), 4, 5, p(ids), p(dists), None)
+    assert rc == N.SSG_EINVAL and "aligned" in N.last_error(None)
+    rc = L.ssg_knn_noalloc(N.METRIC_SQL2, p(dX), 8, 1000, p(dQ, 2), 4, 5, p(ids), p(dists), None)
+    assert rc == N.SSG_EINVAL and "aligned" in N.last_error(None)
+    rc = L.ssg_knn_noalloc(N.METRIC_SQL2, p(dX), 8, 1000, p(dQ), 4, 5, p(ids, 1), p(dists), None)
+    assert rc == N.SSG_EINVAL and "aligned" in N.last_error(None)
