@@ -176,12 +176,15 @@ int ssg_version(void);
 
 /* ---- learned shortlist (no counterpart in the reference) ----
  * ssg_train_mlp trains a network d -> hidden (ReLU) -> out_dim on the index's
- * own data: a seeded sample of `sample_n` objects, their exact 10 nearest
+ * own data: a seeded sample of `sample_n` objects, their exact 50 nearest
  * neighbours within the sample (this library's allknn), `triplets` triplets
- * (anchor, one of those neighbours, a random object of the sample) and the
- * triplet loss max(0, |f(a)-f(p)|^2 - |f(a)-f(n)|^2 + 1), minimised with Adam
- * (learning rate `lr`) for `epochs` passes in mini-batches of `batch`; BF16
- * operands, FP32 accumulation and FP32 master weights.  hidden == 0 gives a
+ * (anchor; one of its 10 nearest as the positive; as the negative, with
+ * probability "train_hard" (default 0.5) one of its neighbours ranked 11..50,
+ * else a uniform object of the sample) and the triplet loss
+ * max(0, |f(a)-f(p)|^2 - |f(a)-f(n)|^2 + 1), minimised with Adam (learning
+ * rate `lr`) for `epochs` passes in mini-batches of `batch`; every product
+ * on the tensor cores with BF16 operands, FP32 accumulation and FP32 master
+ * weights.  hidden == 0 gives a
  * seeded Gaussian random projection d -> out_dim and no training: the
  * baseline the network is measured against.  The database is then embedded
  * and indexed.  From then on ssg_search / ssg_search_device shortlist the
@@ -194,7 +197,7 @@ int ssg_version(void);
  * last search took the learned path.  Float metrics only; 1 <= out_dim <= 256,
  * hidden <= 8192.
  * Readable keys: "learned_recall", "learned_ready", "train_loss",
- * "train_seconds", "train_steps", "shortlist". */
+ * "train_seconds", "train_steps", "shortlist", "train_hard". */
 int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t epochs,
                   int32_t hidden, int32_t out_dim, int32_t batch, double lr, uint64_t seed);
 /* Model files: "SSGMLP01", int64 d, hidden, out_dim, then the FP32 weights
@@ -202,10 +205,12 @@ int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t ep
  * hidden == 0).  Loading embeds and indexes the database again. */
 int ssg_save_model(ssg_index *idx, const char *path);
 int ssg_load_model(ssg_index *idx, const char *path);
-/* One FP32 forward + backward pass of the network on a host batch X of
- * 3*batch rows (anchors, positives, negatives) with host weights; writes the
- * mean triplet loss (margin `margin`) and the weight gradients to host
- * buffers.  For testing the training kernels against a CPU reference. */
+/* One forward + backward pass of the network on a host batch X of 3*batch
+ * rows (anchors, positives, negatives) with host weights, through the
+ * training step's tensor-core kernels with each operand carried as three BF16
+ * pieces (FP32-class accuracy); writes the mean triplet loss (margin
+ * `margin`) and the weight gradients to host buffers.  For testing the
+ * training kernels against a CPU reference. */
 int ssg_mlp_grad_check(int64_t d, int64_t hidden, int64_t out_dim, const float *W1,
                        const float *b1, const float *W2, const float *b2, const float *X,
                        int32_t batch, float margin, float *loss, float *gW1, float *gb1,

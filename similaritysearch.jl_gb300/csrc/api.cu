@@ -90,6 +90,8 @@ struct ssg_index {
     int64_t loc_n = -1;
     int locality_param = 1;
     int wide_param = 1;    // BF16 scan: 256-row database tiles per MMA
+    int64_t wave_param = 0;  // wide scan: query tiles per launch (0: one launch)
+    int pair_param = 0;      // wide scan on CTA pairs (M = 256 MMAs, half the database traffic per SM)
     // K-streaming tensor-core path (FP8 mode, and BF16 for dim > 256): operand
     // tiles, per-row FP8 scales, per-row epilogue coefficients, query tiles
     DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
@@ -110,6 +112,7 @@ struct ssg_index {
     ssg::LearnedModel *learned = nullptr;
     int learned_param = 1;
     double learned_target = 0.99;
+    double train_hard = 0.5;  // share of semi-hard negatives in training triplets
     int last_learned = 0;
     float max_x_sq = 0.0f;
     int margin_param = 0;
@@ -790,7 +793,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     idx->last_fallbacks = 0;
     // more candidates than the scans' on-chip heaps hold: threshold filter
     // (the wide scan, one query tile per CTA, is chosen first when it fits)
-    const bool wide = idx->wide_param && ssg::tc_wide_fits(kp, kk);
+    const bool wide = idx->wide_param && (ssg::tc_wide_fits(kp, kk) || (idx->pair_param && ssg::tc_pair_fits(kp, kk)));
     if (wide) qt = 1;
     else if (!ssg::tc_choose(kp, kk, &qt, &stages))
         return run_knn_tc_filter(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db, kk);
@@ -825,7 +828,8 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         rot = static_cast<const int *>(idx->loc_rot.p);
     }
     if (!queries_are_db) {
-        const int64_t qt_alloc = (m + qrows - 1) / qrows * qt;
+        // an even number of tiles: the pair scan reads query tiles in pairs
+        const int64_t qt_alloc = ((m + qrows - 1) / qrows * qt + 1) / 2 * 2;
         SSG_CK(idx->tc_q.ensure(size_t(qt_alloc) * tb), "allocating BF16 query tiles");
         SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(dq), m, idx->dim, qt_alloc,
                                       static_cast<uint8_t *>(idx->tc_q.p), idx->stream, &idx->last_launches),
@@ -838,7 +842,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, idx->dim,
                                    kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
                                    static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
-                                   perm, rot, idx->wide_param != 0),
+                                   perm, rot, idx->wide_param != 0, idx->wave_param, idx->pair_param != 0),
                "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
@@ -946,7 +950,7 @@ int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t 
     const size_t tb = ssg::tc_tile_bytes(idx->dim);
     const uint8_t *qtiles = static_cast<const uint8_t *>(idx->tc_db.p);
     if (!queries_are_db) {
-        const int64_t qt_alloc = (m + 127) / 128;
+        const int64_t qt_alloc = ((m + 127) / 128 + 1) / 2 * 2;  // even: the sample scan may run on CTA pairs
         SSG_CK(idx->tc_q.ensure(size_t(qt_alloc) * tb), "allocating BF16 query tiles");
         SSG_CK(ssg::launch_bf16_tiles(static_cast<const float *>(dq), m, idx->dim, qt_alloc,
                                       static_cast<uint8_t *>(idx->tc_q.p), idx->stream, &idx->last_launches),
@@ -970,7 +974,7 @@ int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t 
             SSG_CK(ssg::launch_tc_scan(idx->metric, qc_tiles, static_cast<const uint8_t *>(idx->tc_smp.p),
                                        static_cast<const float *>(idx->tc_smp_norm.p), idx->smp_rows, mc, idx->dim,
                                        kSampleK, 1, cand, status, idx->stream, &idx->last_launches, nullptr,
-                                       nullptr, nullptr, true),
+                                       nullptr, nullptr, true, 0, idx->pair_param != 0),
                    "launching the sample scan");
             SSG_CK(ssg::launch_sample_bound(cand, mc, segs_s, kSampleK, thr, idx->stream, &idx->last_launches),
                    "computing filter bounds");
@@ -1239,7 +1243,8 @@ bool graph_capturable(ssg_index *idx, int k) {
     if (uses_stream(idx)) return true;
     int qt = 0, stages = 0;
     const int kp = ssg::tc_padded_k(idx->dim), kk = int(overfetch_kk(idx, k));
-    return (idx->wide_param && ssg::tc_wide_fits(kp, kk)) || ssg::tc_choose(kp, kk, &qt, &stages);
+    return (idx->wide_param && (ssg::tc_wide_fits(kp, kk) || (idx->pair_param && ssg::tc_pair_fits(kp, kk)))) ||
+           ssg::tc_choose(kp, kk, &qt, &stages);
 }
 
 // Everything a captured graph depends on: shape, method, tunables and the
@@ -1249,7 +1254,8 @@ std::vector<uint64_t> graph_key(const ssg_index *idx, int64_t m, int k) {
     static_assert(sizeof(double) == 8, "double");
     memcpy(&of, &idx->overfetch, 8);
     std::vector<uint64_t> key = {uint64_t(m), uint64_t(k), uint64_t(idx->n), uint64_t(idx->prec),
-                                 uint64_t(idx->metric), of, uint64_t(idx->splits_param), uint64_t(idx->wide_param)};
+                                 uint64_t(idx->metric), of, uint64_t(idx->splits_param), uint64_t(idx->wide_param),
+                                 uint64_t(idx->wave_param), uint64_t(idx->pair_param)};
     for (const DevBuf *b : {&idx->db, &idx->db_norm, &idx->tc_db, &idx->tc_norm, &idx->tc_q, &idx->st_db,
                             &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale, &idx->cand,
                             &idx->red[0], &idx->red[1], &idx->status, &idx->gbound, &idx->qnorm, &idx->pack_q,
@@ -1654,6 +1660,9 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
     } else if (k == "learned_target") {
         if (!(value >= 0.0 && value <= 1.0)) return fail(idx, SSG_EINVAL, "learned_target must be in [0, 1]");
         idx->learned_target = value;
+    } else if (k == "train_hard") {
+        if (!(value >= 0.0 && value <= 1.0)) return fail(idx, SSG_EINVAL, "train_hard must be in [0, 1]");
+        idx->train_hard = value;
     } else if (k == "shortlist") {
         if (!(value >= 1 && value <= 4096)) return fail(idx, SSG_EINVAL, "shortlist must be in [1, 4096]");
         if (!ssg::learned_set(idx->learned, "shortlist", value))
@@ -1667,6 +1676,11 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->locality_param = value != 0.0;
     } else if (k == "wide") {
         idx->wide_param = value != 0.0;
+    } else if (k == "pair") {
+        idx->pair_param = value != 0.0;
+    } else if (k == "wave") {
+        if (!(value >= 0 && value <= 1e6)) return fail(idx, SSG_EINVAL, "wave out of range");
+        idx->wave_param = int64_t(value);
     } else if (k == "profile") {
         idx->profile = value != 0.0;
         if (idx->profile) { idx->main_ms = 0.0; idx->main_launches = 0; }
@@ -1689,6 +1703,8 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "profile") *value = idx->profile;
     else if (k == "locality") *value = idx->locality_param;
     else if (k == "wide") *value = idx->wide_param;
+    else if (k == "wave") *value = double(idx->wave_param);
+    else if (k == "pair") *value = idx->pair_param;
     else if (k == "graphs") *value = idx->graphs_param;
     else if (k == "graph_replays") *value = double(idx->graph_replays);
     else if (k == "last_graph") *value = idx->last_graph;
@@ -1700,6 +1716,7 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "plain") *value = idx->plain_param;
     else if (k == "learned") *value = idx->learned_param;
     else if (k == "learned_target") *value = idx->learned_target;
+    else if (k == "train_hard") *value = idx->train_hard;
     else if (k == "learned_used") *value = idx->last_learned;
     else if (k == "fallbacks") *value = idx->last_fallbacks;
     else if (k == "max_x_sq") *value = idx->max_x_sq;
@@ -1858,6 +1875,7 @@ int ssg_train_mlp(ssg_index *idx, int64_t sample_n, int64_t triplets, int32_t ep
     t.margin = 1.0f;
     t.seed = seed;
     t.shortlist = 512;
+    t.hard = float(idx->train_hard);
     ssg::LearnedModel *m = nullptr;
     std::string err;
     int rc = ssg::learned_train(view_of(idx), t, &m, err);

@@ -100,8 +100,10 @@ int64_t tc_tiles(int64_t rows);
 size_t tc_tile_bytes(int64_t dim);
 // Chooses query tiles per CTA and pipeline depth; false if kk cannot fit.
 bool tc_choose(int kp, int kk, int *qt, int *stages);
-// Whether the wide scan's heaps and ring fit for this K and candidate count.
+// Whether the wide scan's heaps and ring fit for this K and candidate count
+// (one CTA, or a CTA pair with half-size ring stages).
 bool tc_wide_fits(int kp, int kk);
+bool tc_pair_fits(int kp, int kk);
 // Sorted candidate segments the scan writes per (query, split) for a CTA with
 // `qt` query tiles (the epilogue splits a tile's columns between warps).
 int tc_segments_per_split(int qt);
@@ -119,11 +121,13 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
 // tiles built in a locality order, one launch for all queries): perm[p] is
 // the id of the row at position p of both tile sets, query CTA x starts at
 // database tile rot[x], keys carry ids and each query's candidates go to
-// the row of its id.
+// the row of its id.  wave > 0: the wide scan is launched `wave` query tiles
+// at a time.  pair (with wide): the scan runs on CTA pairs with M = 256 MMAs
+// (the query tile set must then hold an even number of tiles).
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm = nullptr,
-                           const int *rot = nullptr, bool wide = false);
+                           const int *rot = nullptr, bool wide = false, int64_t wave = 0, bool pair = false);
 // Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
 // segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
 // grouped by pivot) and rot (start tile of each query tile's scan).
@@ -203,16 +207,46 @@ cudaError_t launch_scatter_results(const uint32_t *src_ids, const float *src_d, 
 int device_sm_count();
 
 // ---- learned shortlist (mlp.cu, learned.cu) ----
-// C[M x N] = op(A) op(B) (+bias) (ReLU): op(A) = A (M x K) or A^T (A is K x M,
-// ta); op(B) = B^T (B is N x K) or B (B is K x N, tb); bf16 rounds operands.
-cudaError_t mlp_gemm(const float *A, const float *B, const float *bias, float *C, int M, int N, int K, int ta, int tb,
-                     int relu, int bf16, int accumulate, cudaStream_t st, int *launches);
+// C (M x N, row-major, row stride ldc) = A B^T on the tensor cores, A = M x K
+// and B = N x K given K-major (X[r * ld + k]) or transposed (X[k * ld + r]),
+// FP32 in memory, BF16 operands, FP32 accumulation.  Epilogue: + bias[n],
+// ReLU, * (mask[m * ldc + n] > 0), per-M-tile column sums
+// colsum[tile * N + n].  splits > 1 splits K: part s is written at
+// C + s * M * ldc (no epilogue then).  exact: operands as three BF16 pieces
+// and six piece products (FP32-class accuracy, ~2^-24).  *err receives a
+// non-zero code if a bounded wait gave up.
+struct MlpGemm {
+    const float *A = nullptr;
+    int64_t lda = 0;
+    int a_kmajor = 1;
+    const float *B = nullptr;
+    int64_t ldb = 0;
+    int b_kmajor = 1;
+    float *C = nullptr;
+    int64_t ldc = 0;
+    int M = 0, N = 0, K = 0;
+    int splits = 1;
+    const float *bias = nullptr;
+    int relu = 0;
+    const float *mask = nullptr;
+    float *colsum = nullptr;
+    int exact = 0;
+    int *err = nullptr;
+};
+cudaError_t mlp_gemm(const MlpGemm &g, cudaStream_t st, int *launches);
+int mlp_gemm_mtiles(int M);  // M tiles = rows of the column-sum partials
 cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
                         cudaStream_t st, int *launches);
-cudaError_t mlp_relu_backward(float *dH, const float *H, int64_t count, cudaStream_t st, int *launches);
-cudaError_t mlp_colsum(const float *G, int rows, int N, float *out, cudaStream_t st, int *launches);
-cudaError_t mlp_adam(float *W, const float *G, float *M, float *V, int64_t count, float lr, int step,
+// out[p * N + n] = sum of G[r][n] over the p-th of `parts` row ranges
+cudaError_t mlp_colsum_parts(const float *G, int rows, int N, int parts, float *out, cudaStream_t st, int *launches);
+// out[i] = sum over p < parts of G[p * count + i]
+cudaError_t mlp_sum_parts(const float *G, int parts, int64_t count, float *out, cudaStream_t st, int *launches);
+// Adam step on W; the gradient is the sum of `parts` partials G[p * count + i]
+cudaError_t mlp_adam(float *W, const float *G, int parts, float *M, float *V, int64_t count, float lr, int step,
                      cudaStream_t st, int *launches);
+// X = [S[idx[off..]]; S[idx[T + off..]]; S[idx[2T + off..]]] (bb rows each)
+cudaError_t mlp_gather3(const float *S, const int64_t *idx, int64_t T, int64_t off, int bb, int d, float *X,
+                        cudaStream_t st, int *launches);
 
 // What the learned code needs of an index.
 struct IndexView {
@@ -231,6 +265,9 @@ struct TrainArgs {
     float lr, margin;
     uint64_t seed;
     int shortlist;
+    // fraction of negatives drawn from the anchor's exact neighbours just
+    // beyond the positives (ranks 11..50 in the sample), the rest uniform
+    float hard;
 };
 struct LearnedModel;
 void learned_free(LearnedModel *m);

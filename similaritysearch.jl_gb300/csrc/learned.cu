@@ -43,6 +43,7 @@ struct LearnedModel {
     uint32_t *cand_ids = nullptr;
     float *cand_d = nullptr;
     size_t zq_rows = 0, cand_rows = 0;
+    int *dev_err = nullptr;  // status word of the tensor-core GEMMs' bounded waits
 };
 
 namespace {
@@ -65,21 +66,56 @@ struct Cuda {
 void free_model_buffers(LearnedModel *m) {
     for (float *p : {m->W1, m->b1, m->W2, m->b2, m->zq, m->hq, m->cand_d}) if (p) cudaFree(p);
     if (m->cand_ids) cudaFree(m->cand_ids);
+    if (m->dev_err) cudaFree(m->dev_err);
     m->W1 = m->b1 = m->W2 = m->b2 = m->zq = m->hq = m->cand_d = nullptr;
     m->cand_ids = nullptr;
+    m->dev_err = nullptr;
     m->zq_rows = m->cand_rows = 0;
     if (m->sub) ssg_destroy(m->sub);
     m->sub = nullptr;
 }
 
 // Z (rows x E) = f(X) for rows of X (d floats); Hs is rows x H scratch.
-int embed_rows(LearnedModel *m, const float *X, int64_t rows, float *Z, float *Hs, cudaStream_t st, Cuda &cu,
+// Tensor-core products with BF16 operands, as in training.
+int embed_rows(LearnedModel *m, const float *X, int64_t rows, float *Z, float *Hs, int *err, cudaStream_t st, Cuda &cu,
                int *launches) {
+    MlpGemm g;
+    g.err = err;
+    g.M = int(rows);
     if (m->H > 0) {
-        LK(mlp_gemm(X, m->W1, m->b1, Hs, int(rows), int(m->H), int(m->d), 0, 0, 1, 1, 0, st, launches), "embedding");
-        LK(mlp_gemm(Hs, m->W2, m->b2, Z, int(rows), int(m->E), int(m->H), 0, 0, 0, 1, 0, st, launches), "embedding");
+        g.A = X; g.lda = m->d; g.B = m->W1; g.ldb = m->d; g.C = Hs; g.ldc = m->H;
+        g.N = int(m->H); g.K = int(m->d); g.bias = m->b1; g.relu = 1;
+        LK(mlp_gemm(g, st, launches), "embedding");
+        g.A = Hs; g.lda = m->H; g.B = m->W2; g.ldb = m->H; g.C = Z; g.ldc = m->E;
+        g.N = int(m->E); g.K = int(m->H); g.bias = m->b2; g.relu = 0;
+        LK(mlp_gemm(g, st, launches), "embedding");
     } else {
-        LK(mlp_gemm(X, m->W1, nullptr, Z, int(rows), int(m->E), int(m->d), 0, 0, 0, 1, 0, st, launches), "embedding");
+        g.A = X; g.lda = m->d; g.B = m->W1; g.ldb = m->d; g.C = Z; g.ldc = m->E;
+        g.N = int(m->E); g.K = int(m->d);
+        LK(mlp_gemm(g, st, launches), "embedding");
+    }
+    return SSG_OK;
+}
+
+// The model's device status word (zeroed); null after an allocation failure.
+int *err_word(LearnedModel *m, Cuda &cu) {
+    if (!m->dev_err) {
+        void *p = nullptr;
+        if (!cu.ok(cudaMalloc(&p, sizeof(int)), "allocating a status word")) return nullptr;
+        m->dev_err = static_cast<int *>(p);
+    }
+    if (!cu.ok(cudaMemset(m->dev_err, 0, sizeof(int)), "clearing a status word")) return nullptr;
+    return m->dev_err;
+}
+
+// After a synchronisation: SSG_ETIMEOUT if a bounded wait of the GEMMs gave up.
+int check_err_word(LearnedModel *m, Cuda &cu) {
+    int h = 0;
+    if (!cu.ok(cudaMemcpy(&h, m->dev_err, sizeof(int), cudaMemcpyDeviceToHost), "reading a status word"))
+        return SSG_ECUDA;
+    if (h != 0) {
+        cu.err = "a bounded wait in the network's tensor-core GEMM gave up (code " + std::to_string(h) + ")";
+        return SSG_ETIMEOUT;
     }
     return SSG_OK;
 }
@@ -126,11 +162,14 @@ int learned_index_db(LearnedModel *m, const IndexView &v, std::string &err) {
     float *Hs = m->H > 0 ? dmalloc(size_t(chunk) * m->H, cu, "allocating hidden scratch") : nullptr;
     if (!Z || (m->H > 0 && !Hs)) { err = cu.err; if (Z) cudaFree(Z); return SSG_ENOMEM; }
     int rc = SSG_OK;
+    int *ew = err_word(m, cu);
+    if (!ew) rc = SSG_ECUDA;
     for (int64_t r0 = 0; r0 < v.n && rc == SSG_OK; r0 += chunk) {
         const int64_t rows = std::min(chunk, v.n - r0);
-        rc = embed_rows(m, v.db + size_t(r0) * v.dim, rows, Z + size_t(r0) * m->E, Hs, v.stream, cu, v.launches);
+        rc = embed_rows(m, v.db + size_t(r0) * v.dim, rows, Z + size_t(r0) * m->E, Hs, ew, v.stream, cu, v.launches);
     }
     if (rc == SSG_OK && !cu.ok(cudaStreamSynchronize(v.stream), "embedding the database")) rc = SSG_ECUDA;
+    if (rc == SSG_OK) rc = check_err_word(m, cu);
     if (rc == SSG_OK) {
         if (m->sub) ssg_destroy(m->sub);
         m->sub = nullptr;
@@ -174,9 +213,13 @@ int learned_search(LearnedModel *m, const IndexView &v, const float *dq, const f
         if (!m->cand_d) { err = cu.err; return SSG_ENOMEM; }
         m->cand_rows = size_t(mq) * S;
     }
-    int rc = embed_rows(m, dq, mq, m->zq, m->hq, v.stream, cu, v.launches);
+    int *ew = err_word(m, cu);
+    if (!ew) { err = cu.err; return SSG_ECUDA; }
+    int rc = embed_rows(m, dq, mq, m->zq, m->hq, ew, v.stream, cu, v.launches);
     if (rc) { err = cu.err; return rc; }
     if (!cu.ok(cudaStreamSynchronize(v.stream), "embedding queries")) { err = cu.err; return SSG_ECUDA; }
+    rc = check_err_word(m, cu);
+    if (rc) { err = cu.err; return rc; }
     rc = ssg_search_device(m->sub, m->zq, mq, S, m->cand_ids, m->cand_d, 0);
     if (rc) {
         char buf[256];
@@ -251,13 +294,18 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
         LK(launch_gather_rows(v.db, d_sample, ns, size_t(d) * 4, S, v.stream, v.launches), "gathering the sample");
         LK(cudaStreamSynchronize(v.stream), "gathering the sample");
         cudaFree(d_sample);
-        // 2. exact 10-NN of every sampled object (self excluded) with this library
+        // 2. exact nearest neighbours of every sampled object (self excluded)
+        // with this library: 10 positives, and 40 more ranks for the
+        // semi-hard negatives when t.hard > 0
+        const int KP = int(std::min<int64_t>(10, ns - 1));
+        const int KN = t.hard > 0.0f ? int(std::min<int64_t>(40, ns - 1 - KP)) : 0;
+        const int KA = KP + KN;
         ssg_index *tmp = nullptr;
         int rc = ssg_create_device(v.metric, SSG_ELEM_F32, d, ns, S, d, SSG_PREC_FP32, &tmp);
         if (rc) { cudaFree(S); err = "sample index creation failed"; learned_free(m); return rc; }
         uint32_t *nn_ids = nullptr;
         float *nn_d = nullptr;
-        if (cudaMalloc(&nn_ids, size_t(ns) * 10 * 4) != cudaSuccess || cudaMalloc(&nn_d, size_t(ns) * 10 * 4) != cudaSuccess) {
+        if (cudaMalloc(&nn_ids, size_t(ns) * KA * 4) != cudaSuccess || cudaMalloc(&nn_d, size_t(ns) * KA * 4) != cudaSuccess) {
             cudaGetLastError();
             if (nn_ids) cudaFree(nn_ids);
             ssg_destroy(tmp);
@@ -266,40 +314,62 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
             learned_free(m);
             return SSG_ENOMEM;
         }
-        rc = ssg_allknn_device(tmp, 10, 1, nn_ids, nn_d);
-        std::vector<uint32_t> nn(size_t(ns) * 10);
+        rc = ssg_allknn_device(tmp, KA, 1, nn_ids, nn_d);
+        std::vector<uint32_t> nn(size_t(ns) * KA);
         if (!rc) cudaMemcpy(nn.data(), nn_ids, nn.size() * 4, cudaMemcpyDeviceToHost);
         ssg_destroy(tmp);
         cudaFree(nn_ids);
         cudaFree(nn_d);
         if (rc) { cudaFree(S); err = "allknn over the sample failed"; learned_free(m); return rc; }
-        // 3. triplets (indices into the sample)
+        // 3. triplets (indices into the sample): anchor, one of its KP exact
+        // neighbours, and a negative -- with probability t.hard one of its
+        // neighbours ranked KP+1 .. KP+KN (close but farther than every
+        // positive: the anchor's neighbourhood must be ordered, not only
+        // separated from far objects), otherwise a uniform object
         const int64_t T = t.triplets;
         std::vector<int64_t> trip(size_t(3 * T));
         std::uniform_int_distribution<int64_t> ua(0, ns - 1);
-        std::uniform_int_distribution<int> ur(0, 9);
+        std::uniform_int_distribution<int> ur(0, KP - 1);
+        std::uniform_int_distribution<int> uh(0, std::max(0, KN - 1));
+        std::uniform_real_distribution<float> u01(0.0f, 1.0f);
         for (int64_t i = 0; i < T; ++i) {
             const int64_t a = ua(rng);
-            uint32_t p = nn[size_t(a) * 10 + size_t(ur(rng))];
+            uint32_t p = nn[size_t(a) * KA + size_t(ur(rng))];
             if (p == 0) p = uint32_t(a + 1);  // unfilled slot: the anchor itself
+            int64_t neg = -1;
+            if (KN > 0 && u01(rng) < t.hard) {
+                const uint32_t h = nn[size_t(a) * KA + KP + size_t(uh(rng))];
+                if (h != 0) neg = int64_t(h) - 1;
+            }
+            if (neg < 0) neg = ua(rng);
             trip[size_t(i)] = a;
             trip[size_t(T + i)] = int64_t(p) - 1;
-            trip[size_t(2 * T + i)] = ua(rng);
+            trip[size_t(2 * T + i)] = neg;
         }
         int64_t *d_trip = nullptr;
         LK(cudaMalloc(&d_trip, trip.size() * 8), "allocating triplets");
         cudaMemcpy(d_trip, trip.data(), trip.size() * 8, cudaMemcpyHostToDevice);
-        // 4. training buffers
+        // 4. training buffers.  One step: X = the batch's anchors, positives
+        // and negatives (3B rows), H = relu(X W1^T + b1), Z = H W2^T + b2,
+        // the loss and dZ, gW2 = dZ^T H (split K), dH = (dZ W2) * (H > 0)
+        // with its per-tile column sums (gb1), gW1 = dH^T X (split K), the
+        // column sums of dZ (gb2), then Adam summing each gradient's parts in
+        // a fixed order.  All products on the tensor cores (mlp.cu).
         const int B = t.batch;
-        const size_t R = size_t(3) * B;
-        float *X = dmalloc(R * d, cu, "x"), *Hh = dmalloc(R * H, cu, "h"), *Z = dmalloc(R * E, cu, "z");
-        float *dZ = dmalloc(R * E, cu, "dz"), *dH = dmalloc(R * H, cu, "dh");
-        float *gW1 = dmalloc(size_t(H) * d, cu, "g"), *gb1 = dmalloc(size_t(H), cu, "g");
-        float *gW2 = dmalloc(size_t(E) * H, cu, "g"), *gb2 = dmalloc(size_t(E), cu, "g");
+        const int R = 3 * B;
+        const int mt = mlp_gemm_mtiles(R);                 // row tiles: parts of gb1
+        const int s1 = std::max(1, std::min(16, R / 384)); // K splits of gW1 (M = H, N = d)
+        const int s2 = std::max(1, std::min(16, R / 256)); // K splits of gW2 (M = E, N = H)
+        const int pb2 = std::max(1, std::min(32, R / 96)); // row ranges of gb2's column sums
+        float *X = dmalloc(size_t(R) * d, cu, "x"), *Hh = dmalloc(size_t(R) * H, cu, "h"), *Z = dmalloc(size_t(R) * E, cu, "z");
+        float *dZ = dmalloc(size_t(R) * E, cu, "dz"), *dH = dmalloc(size_t(R) * H, cu, "dh");
+        float *gW1 = dmalloc(size_t(s1) * H * d, cu, "g"), *gb1 = dmalloc(size_t(mt) * H, cu, "g");
+        float *gW2 = dmalloc(size_t(s2) * E * H, cu, "g"), *gb2 = dmalloc(size_t(pb2) * E, cu, "g");
         const size_t npar = size_t(H) * d + H + size_t(E) * H + E;
         float *mom = dmalloc(2 * npar, cu, "adam");
         float *stat = dmalloc(2, cu, "loss");
-        if (!X || !Hh || !Z || !dZ || !dH || !gW1 || !gb1 || !gW2 || !gb2 || !mom || !stat) {
+        int *ew = err_word(m, cu);
+        if (!X || !Hh || !Z || !dZ || !dH || !gW1 || !gb1 || !gW2 || !gb2 || !mom || !stat || !ew) {
             for (float *p : {X, Hh, Z, dZ, dH, gW1, gb1, gW2, gb2, mom, stat})
                 if (p) cudaFree(p);
             cudaFree(S); cudaFree(d_trip);
@@ -314,34 +384,47 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
         for (int ep = 0; ep < t.epochs && status == SSG_OK; ++ep) {
             for (int64_t s = 0; s < steps_per_epoch && status == SSG_OK; ++s) {
                 const int64_t off = (s * B) % T;
-                const int64_t bb = std::min<int64_t>(B, T - off);
-                // X = [anchors; positives; negatives] of this batch
-                for (int part = 0; part < 3; ++part)
-                    if (!cu.ok(launch_gather_rows(S, d_trip + part * T + off, bb, size_t(d) * 4,
-                                                  X + size_t(part) * bb * d, v.stream, v.launches),
-                               "gathering a batch")) status = SSG_ECUDA;
-                const int rows = int(3 * bb);
+                const int bb = int(std::min<int64_t>(B, T - off));
+                const int rows = 3 * bb;
                 ++step;
-                cudaMemsetAsync(stat, 0, 8, v.stream);
-                bool ok = cu.ok(mlp_gemm(X, m->W1, m->b1, Hh, rows, int(H), int(d), 0, 0, 1, 1, 0, v.stream, v.launches), "fwd") &&
-                          cu.ok(mlp_gemm(Hh, m->W2, m->b2, Z, rows, int(E), int(H), 0, 0, 0, 1, 0, v.stream, v.launches), "fwd") &&
-                          cu.ok(mlp_triplet(Z, int(bb), int(E), t.margin, dZ, stat, reinterpret_cast<int *>(stat + 1),
+                MlpGemm f1, f2, gw2, dh, gw1;
+                f1.err = f2.err = gw2.err = dh.err = gw1.err = ew;
+                // H = relu(X W1^T + b1)
+                f1.A = X; f1.lda = d; f1.B = m->W1; f1.ldb = d; f1.C = Hh; f1.ldc = H;
+                f1.M = rows; f1.N = int(H); f1.K = int(d); f1.bias = m->b1; f1.relu = 1;
+                // Z = H W2^T + b2
+                f2.A = Hh; f2.lda = H; f2.B = m->W2; f2.ldb = H; f2.C = Z; f2.ldc = E;
+                f2.M = rows; f2.N = int(E); f2.K = int(H); f2.bias = m->b2;
+                // gW2 (E x H) = dZ^T H: both operands transposed, K = rows
+                gw2.A = dZ; gw2.lda = E; gw2.a_kmajor = 0; gw2.B = Hh; gw2.ldb = H; gw2.b_kmajor = 0;
+                gw2.C = gW2; gw2.ldc = H; gw2.M = int(E); gw2.N = int(H); gw2.K = rows; gw2.splits = s2;
+                // dH = (dZ W2) * (H > 0), column sums per row tile (gb1)
+                dh.A = dZ; dh.lda = E; dh.B = m->W2; dh.ldb = H; dh.b_kmajor = 0; dh.C = dH; dh.ldc = H;
+                dh.M = rows; dh.N = int(H); dh.K = int(E); dh.mask = Hh; dh.colsum = gb1;
+                // gW1 (H x d) = dH^T X, K = rows
+                gw1.A = dH; gw1.lda = H; gw1.a_kmajor = 0; gw1.B = X; gw1.ldb = d; gw1.b_kmajor = 0;
+                gw1.C = gW1; gw1.ldc = d; gw1.M = int(H); gw1.N = int(d); gw1.K = rows; gw1.splits = s1;
+                const int mt_b = mlp_gemm_mtiles(rows);
+                bool ok = cu.ok(mlp_gather3(S, d_trip, T, off, bb, int(d), X, v.stream, v.launches), "gathering a batch") &&
+                          cu.ok(cudaMemsetAsync(stat, 0, 8, v.stream), "loss") &&
+                          cu.ok(mlp_gemm(f1, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_gemm(f2, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_triplet(Z, bb, int(E), t.margin, dZ, stat, reinterpret_cast<int *>(stat + 1),
                                             v.stream, v.launches), "loss") &&
-                          cu.ok(mlp_gemm(dZ, Hh, nullptr, gW2, int(E), int(H), rows, 1, 1, 0, 1, 0, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_colsum(dZ, rows, int(E), gb2, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_gemm(dZ, m->W2, nullptr, dH, rows, int(H), int(E), 0, 1, 0, 1, 0, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_relu_backward(dH, Hh, int64_t(rows) * H, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_gemm(dH, X, nullptr, gW1, int(H), int(d), rows, 1, 1, 0, 1, 0, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_colsum(dH, rows, int(H), gb1, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_adam(m->W1, gW1, mW1, vW1, int64_t(H) * d, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->b1, gb1, mb1, vb1, H, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->W2, gW2, mW2, vW2, int64_t(E) * H, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->b2, gb2, mb2, vb2, E, t.lr, int(step), v.stream, v.launches), "adam");
+                          cu.ok(mlp_gemm(gw2, v.stream, v.launches), "bwd") &&
+                          cu.ok(mlp_colsum_parts(dZ, rows, int(E), pb2, gb2, v.stream, v.launches), "bwd") &&
+                          cu.ok(mlp_gemm(dh, v.stream, v.launches), "bwd") &&
+                          cu.ok(mlp_gemm(gw1, v.stream, v.launches), "bwd") &&
+                          cu.ok(mlp_adam(m->W1, gW1, s1, mW1, vW1, int64_t(H) * d, t.lr, int(step), v.stream, v.launches), "adam") &&
+                          cu.ok(mlp_adam(m->b1, gb1, mt_b, mb1, vb1, H, t.lr, int(step), v.stream, v.launches), "adam") &&
+                          cu.ok(mlp_adam(m->W2, gW2, s2, mW2, vW2, int64_t(E) * H, t.lr, int(step), v.stream, v.launches), "adam") &&
+                          cu.ok(mlp_adam(m->b2, gb2, pb2, mb2, vb2, E, t.lr, int(step), v.stream, v.launches), "adam");
                 if (!ok) status = SSG_ECUDA;
                 if (ok && (s + 1 == steps_per_epoch)) {
                     float loss = 0.0f;
                     cudaMemcpyAsync(&loss, stat, 4, cudaMemcpyDeviceToHost, v.stream);
                     if (!cu.ok(cudaStreamSynchronize(v.stream), "training")) status = SSG_ECUDA;
+                    if (status == SSG_OK) status = check_err_word(m, cu);
                     m->loss_curve.push_back(loss);
                     m->train_loss = loss;
                 }
@@ -425,13 +508,20 @@ int learned_load(const IndexView &v, const char *path, LearnedModel **out, std::
 void learned_set_recall(LearnedModel *m, double r) { m->est_recall = r; }
 
 // One forward + backward pass on a host batch (anchors; positives; negatives)
-// with host weights: the gradient check against the CPU oracle.
+// with host weights: the gradient check against the CPU oracle.  The same
+// kernels and decomposition as a training step (split K, per-tile column
+// sums, parts summed in order), with the GEMMs in exact mode (operands as
+// three BF16 pieces, six piece products), so the result is checked at
+// FP32-class accuracy.
 int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const float *b1, const float *W2,
                        const float *b2, const float *X, int B, float margin, float *loss, float *gW1, float *gb1,
                        float *gW2, float *gb2, std::string &err) {
     Cuda cu;
-    const size_t R = size_t(3) * B;
-    std::vector<float *> bufs;
+    const int R = 3 * B;
+    const int mt = mlp_gemm_mtiles(R);
+    const int s1 = std::max(1, std::min(16, R / 384)), s2 = std::max(1, std::min(16, R / 256));
+    const int pb2 = std::max(1, std::min(32, R / 96));
+    std::vector<void *> bufs;
     auto up = [&](const float *h, size_t n) -> float * {
         float *p = dmalloc(n, cu, "alloc");
         if (p) { bufs.push_back(p); cudaMemcpy(p, h, n * 4, cudaMemcpyHostToDevice); }
@@ -443,25 +533,48 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
         return p;
     };
     float *dW1 = up(W1, size_t(H) * d), *db1 = up(b1, H), *dW2 = up(W2, size_t(E) * H), *db2 = up(b2, E);
-    float *dX = up(X, R * d), *Hh = mk(R * H), *Z = mk(R * E), *dZ = mk(R * E), *dH = mk(R * H);
-    float *g1 = mk(size_t(H) * d), *gb1d = mk(H), *g2 = mk(size_t(E) * H), *gb2d = mk(E), *stat = mk(2);
+    float *dX = up(X, size_t(R) * d), *Hh = mk(size_t(R) * H), *Z = mk(size_t(R) * E), *dZ = mk(size_t(R) * E);
+    float *dH = mk(size_t(R) * H), *p1 = mk(size_t(s1) * H * d), *pb1 = mk(size_t(mt) * H), *p2 = mk(size_t(s2) * E * H);
+    float *pb2d = mk(size_t(pb2) * E), *g1 = mk(size_t(H) * d), *gb1d = mk(H), *g2 = mk(size_t(E) * H);
+    float *gb2d = mk(E), *stat = mk(2);
+    int *ew = reinterpret_cast<int *>(mk(1));
     int rc = SSG_OK;
-    if (!dW1 || !db1 || !dW2 || !db2 || !dX || !Hh || !Z || !dZ || !dH || !g1 || !gb1d || !g2 || !gb2d || !stat)
-        rc = SSG_ENOMEM;
+    for (void *p : {(void *)dW1, (void *)db1, (void *)dW2, (void *)db2, (void *)dX, (void *)Hh, (void *)Z, (void *)dZ,
+                    (void *)dH, (void *)p1, (void *)pb1, (void *)p2, (void *)pb2d, (void *)g1, (void *)gb1d, (void *)g2,
+                    (void *)gb2d, (void *)stat, (void *)ew})
+        if (!p) rc = SSG_ENOMEM;
     cudaStream_t st = nullptr;
-    const int rows = int(R);
     if (!rc) {
         cudaMemset(stat, 0, 8);
-        bool ok = cu.ok(mlp_gemm(dX, dW1, db1, Hh, rows, int(H), int(d), 0, 0, 1, 0, 0, st, nullptr), "fwd") &&
-                  cu.ok(mlp_gemm(Hh, dW2, db2, Z, rows, int(E), int(H), 0, 0, 0, 0, 0, st, nullptr), "fwd") &&
+        cudaMemset(ew, 0, 4);
+        MlpGemm f1, f2, gw2, dh, gw1;
+        f1.err = f2.err = gw2.err = dh.err = gw1.err = ew;
+        f1.exact = f2.exact = gw2.exact = dh.exact = gw1.exact = 1;
+        f1.A = dX; f1.lda = d; f1.B = dW1; f1.ldb = d; f1.C = Hh; f1.ldc = H;
+        f1.M = R; f1.N = int(H); f1.K = int(d); f1.bias = db1; f1.relu = 1;
+        f2.A = Hh; f2.lda = H; f2.B = dW2; f2.ldb = H; f2.C = Z; f2.ldc = E;
+        f2.M = R; f2.N = int(E); f2.K = int(H); f2.bias = db2;
+        gw2.A = dZ; gw2.lda = E; gw2.a_kmajor = 0; gw2.B = Hh; gw2.ldb = H; gw2.b_kmajor = 0;
+        gw2.C = p2; gw2.ldc = H; gw2.M = int(E); gw2.N = int(H); gw2.K = R; gw2.splits = s2;
+        dh.A = dZ; dh.lda = E; dh.B = dW2; dh.ldb = H; dh.b_kmajor = 0; dh.C = dH; dh.ldc = H;
+        dh.M = R; dh.N = int(H); dh.K = int(E); dh.mask = Hh; dh.colsum = pb1;
+        gw1.A = dH; gw1.lda = H; gw1.a_kmajor = 0; gw1.B = dX; gw1.ldb = d; gw1.b_kmajor = 0;
+        gw1.C = p1; gw1.ldc = d; gw1.M = int(H); gw1.N = int(d); gw1.K = R; gw1.splits = s1;
+        bool ok = cu.ok(mlp_gemm(f1, st, nullptr), "fwd") && cu.ok(mlp_gemm(f2, st, nullptr), "fwd") &&
                   cu.ok(mlp_triplet(Z, B, int(E), margin, dZ, stat, reinterpret_cast<int *>(stat + 1), st, nullptr), "loss") &&
-                  cu.ok(mlp_gemm(dZ, Hh, nullptr, g2, int(E), int(H), rows, 1, 1, 0, 0, 0, st, nullptr), "bwd") &&
-                  cu.ok(mlp_colsum(dZ, rows, int(E), gb2d, st, nullptr), "bwd") &&
-                  cu.ok(mlp_gemm(dZ, dW2, nullptr, dH, rows, int(H), int(E), 0, 1, 0, 0, 0, st, nullptr), "bwd") &&
-                  cu.ok(mlp_relu_backward(dH, Hh, int64_t(rows) * H, st, nullptr), "bwd") &&
-                  cu.ok(mlp_gemm(dH, dX, nullptr, g1, int(H), int(d), rows, 1, 1, 0, 0, 0, st, nullptr), "bwd") &&
-                  cu.ok(mlp_colsum(dH, rows, int(H), gb1d, st, nullptr), "bwd") && cu.ok(cudaDeviceSynchronize(), "sync");
+                  cu.ok(mlp_gemm(gw2, st, nullptr), "bwd") &&
+                  cu.ok(mlp_colsum_parts(dZ, R, int(E), pb2, pb2d, st, nullptr), "bwd") &&
+                  cu.ok(mlp_gemm(dh, st, nullptr), "bwd") && cu.ok(mlp_gemm(gw1, st, nullptr), "bwd") &&
+                  cu.ok(mlp_sum_parts(p1, s1, int64_t(H) * d, g1, st, nullptr), "sum") &&
+                  cu.ok(mlp_sum_parts(pb1, mt, H, gb1d, st, nullptr), "sum") &&
+                  cu.ok(mlp_sum_parts(p2, s2, int64_t(E) * H, g2, st, nullptr), "sum") &&
+                  cu.ok(mlp_sum_parts(pb2d, pb2, E, gb2d, st, nullptr), "sum") && cu.ok(cudaDeviceSynchronize(), "sync");
         if (!ok) rc = SSG_ECUDA;
+        int h = 0;
+        if (!rc && cu.ok(cudaMemcpy(&h, ew, 4, cudaMemcpyDeviceToHost), "status") && h != 0) {
+            cu.err = "a bounded wait in the network's tensor-core GEMM gave up";
+            rc = SSG_ETIMEOUT;
+        }
         if (!rc) {
             cudaMemcpy(loss, stat, 4, cudaMemcpyDeviceToHost);
             cudaMemcpy(gW1, g1, size_t(H) * d * 4, cudaMemcpyDeviceToHost);
@@ -470,7 +583,7 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
             cudaMemcpy(gb2, gb2d, size_t(E) * 4, cudaMemcpyDeviceToHost);
         }
     }
-    for (float *p : bufs) cudaFree(p);
+    for (void *p : bufs) cudaFree(p);
     if (rc) err = cu.err;
     return rc;
 }

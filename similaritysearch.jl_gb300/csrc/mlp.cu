@@ -1,12 +1,30 @@
 // mlp.cu -- kernels of the learned shortlist: a small MLP (d -> H (ReLU) -> E)
 // trained with a triplet loss, forward and backward written by hand.
 //
-// The GEMMs are small (H = 256, E = 64) and off the search's hot path, so
-// they are SIMT kernels: 64 x 64 output tiles, 4 x 4 per thread, FP32
-// accumulation.  With `bf16` set, every operand element is rounded to BF16
-// as it is staged (the BF16-operand / FP32-accumulate arithmetic of the
-// tensor cores); weights are kept in FP32 (master copy) and updated by Adam.
+// Every product of the network -- forward, both weight gradients and the
+// hidden-layer gradient -- runs on the 5th-generation tensor cores
+// (tcgen05.mma kind::f16: BF16 operands, FP32 accumulators in TMEM), in one
+// GEMM kernel that covers all of their operand layouts.  Its threads stage
+// the FP32 operands into shared memory as BF16 tiles in the tensor core's
+// swizzled K-major layout (128-byte rows, 128-byte swizzle), reading rows
+// K-contiguously or, for a transposed operand, M-contiguously (coalesced
+// either way), while one thread issues the MMAs of the previous K-block: two
+// stages, an mbarrier per stage signalled by tcgen05.commit.  The epilogue
+// reads the accumulator with tcgen05.ld and applies what the caller fused
+// in: bias, ReLU, a ReLU-derivative mask, and per-tile column sums (the bias
+// gradients, reduced in a fixed order later, so training is deterministic).
+// Weight gradients (K = the batch's 3B rows) split K across CTAs; each split
+// writes its own partial product and Adam sums the parts in order.
+//
+// `exact` mode: each operand element x is split into three BF16 pieces,
+// hi = bf16(x), mid = bf16(x - hi), lo = bf16(x - hi - mid) (24 significant
+// bits, as many as FP32 holds), and six MMAs accumulate every piece product
+// of weight 2^-16 or more: hi.hi + hi.mid + mid.hi + hi.lo + mid.mid + lo.hi
+// (the dropped ones are below 2^-24 relative).  The gradient check runs the
+// same kernels in this mode against an FP64 oracle, at FP32-class accuracy;
+// training and embedding use plain BF16 operands.
 #include "kernels.h"
+#include "tc_ptx.cuh"
 
 #include <cuda_bf16.h>
 
@@ -14,76 +32,204 @@ namespace ssg {
 
 namespace {
 
-constexpr int GT = 64;   // output tile
-constexpr int GK = 16;   // k per stage
+constexpr int BM = 128;          // rows per tile (TMEM lanes)
+constexpr int BK = 64;           // K elements per K-block: one 128-byte BF16 row
+constexpr int SWB = 128;         // swizzle bytes
+constexpr int GT = 128;          // threads per CTA (4 warps: one TMEM lane quarter each)
 
-__device__ __forceinline__ float round_bf16(float v, int bf16) {
-    return bf16 ? __bfloat162float(__float2bfloat16_rn(v)) : v;
+template <int BN, bool EXACT>
+struct GemmSmem {
+    static constexpr int a_bytes = BM * SWB;             // 16 KB
+    static constexpr int b_bytes = BN * SWB;
+    static constexpr int stage = (a_bytes + b_bytes) * (EXACT ? 3 : 1);  // hi (, mid, lo)
+    static constexpr int total = 1024 + 2 * stage + 4 * BN * 4 + 64;
+};
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// C[M x N] = op(A) * op(B) (+ bias[n]) (ReLU?)
-//   op(A) = A (M x K, row-major) or A^T (A stored K x M) when ta
-//   op(B) = B^T (B stored N x K)  or B   (B stored K x N) when tb
-__global__ void __launch_bounds__(256) mlp_gemm_kernel(const float *__restrict__ A, const float *__restrict__ B,
-                                                        const float *__restrict__ bias, float *__restrict__ Cm,
-                                                        int M, int N, int K, int ta, int tb, int relu, int bf16,
-                                                        int accumulate) {
-    __shared__ float sA[GK][GT + 1];
-    __shared__ float sB[GK][GT + 1];
-    const int tid = threadIdx.x;
-    const int tx = tid % 16, ty = tid / 16;
-    const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += GK) {
-        // consecutive threads walk the operand's contiguous dimension: K for
-        // a row-major operand, the rows for a transposed one (coalesced)
-        for (int e = tid; e < GK * GT; e += 256) {
-            {
-                const int kk = ta ? e / GT : e % GK, r = ta ? e % GT : e / GK;
-                const int gm = m0 + r, gk = k0 + kk;
-                float va = 0.0f;
-                if (gm < M && gk < K) va = ta ? A[size_t(gk) * M + gm] : A[size_t(gm) * K + gk];
-                sA[kk][r] = round_bf16(va, bf16);
+// Stages rows [r0, r0 + R) x K-block [k0, k0 + BK) of an FP32 operand into a
+// BF16 tile (hi) and, in exact mode, the tiles of its second and third
+// pieces (mid, lo) at `piece` bytes after it.  kmajor: element (r, k) at
+// X[r * ld + k], else at X[k * ld + r].  Out-of-range elements are 0.
+template <int R, bool EXACT>
+__device__ __forceinline__ void stage_operand(const float *__restrict__ X, int64_t ld, int kmajor, int r0, int rlim,
+                                              int k0, int klim, bool vec4, uint8_t *hi, int piece) {
+    constexpr int CHUNKS = R * (BK / 8);  // 16-byte chunks of 8 BF16
+    for (int c = threadIdx.x; c < CHUNKS; c += GT) {
+        int r, kc;
+        if (kmajor) { r = c / (BK / 8); kc = c % (BK / 8); }
+        else { kc = c / R; r = c % R; }  // consecutive threads: consecutive rows (coalesced)
+        const int gr = r0 + r, gk = k0 + kc * 8;
+        float v[8];
+        if (gr < rlim) {
+            if (kmajor) {
+                const float *p = X + int64_t(gr) * ld + gk;
+                if (vec4 && gk + 8 <= klim) {
+                    const float4 a = *reinterpret_cast<const float4 *>(p);
+                    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+                    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? p[j] : 0.0f;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? X[int64_t(gk + j) * ld + gr] : 0.0f;
             }
-            {
-                const int kk = tb ? e / GT : e % GK, r = tb ? e % GT : e / GK;
-                const int gn = n0 + r, gk = k0 + kk;
-                float vb = 0.0f;
-                if (gn < N && gk < K) vb = tb ? B[size_t(gk) * N + gn] : B[size_t(gn) * K + gk];
-                sB[kk][r] = round_bf16(vb, bf16);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = 0.0f;
+        }
+        __align__(16) __nv_bfloat16 h[8];
+        __align__(16) __nv_bfloat16 md[8];
+        __align__(16) __nv_bfloat16 l[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            h[j] = __float2bfloat16_rn(v[j]);
+            if (EXACT) {
+                const float r1 = v[j] - __bfloat162float(h[j]);  // exact in FP32
+                md[j] = __float2bfloat16_rn(r1);
+                l[j] = __float2bfloat16_rn(r1 - __bfloat162float(md[j]));
             }
         }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < GK; ++kk) {
-            float a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty * 4 + i];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx * 4 + j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int gm = m0 + ty * 4 + i;
-        if (gm >= M) continue;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int gn = n0 + tx * 4 + j;
-            if (gn >= N) continue;
-            float v = acc[i][j];
-            if (bias) v += bias[gn];
-            if (relu) v = fmaxf(v, 0.0f);
-            float *c = Cm + size_t(gm) * N + gn;
-            *c = accumulate ? *c + v : v;
+        const uint32_t off = tc::swizzled_offset(uint32_t(r), uint32_t(kc * 16), SWB);
+        *reinterpret_cast<uint4 *>(hi + off) = *reinterpret_cast<const uint4 *>(h);
+        if (EXACT) {
+            *reinterpret_cast<uint4 *>(hi + piece + off) = *reinterpret_cast<const uint4 *>(md);
+            *reinterpret_cast<uint4 *>(hi + 2 * piece + off) = *reinterpret_cast<const uint4 *>(l);
         }
     }
 }
+
+template <int BN, bool EXACT>
+__global__ void __launch_bounds__(GT, 1) mlp_gemm_kernel(MlpGemm g, int vec_a, int vec_b) {
+    using S = GemmSmem<BN, EXACT>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    float *red = reinterpret_cast<float *>(smem + 2 * S::stage);   // [4][BN] column-sum scratch
+    uint64_t *bar = reinterpret_cast<uint64_t *>(red + 4 * BN);    // one per stage
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 2);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kps = (g.K + int(gridDim.z) - 1) / int(gridDim.z);
+    const int kbeg = int(blockIdx.z) * ((kps + BK - 1) / BK * BK);
+    const int kend = min(g.K, kbeg + (kps + BK - 1) / BK * BK);
+    const int nkb = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::fence_mbarrier_init();
+    }
+    if (warp == 0) tc::tmem_alloc<BN>(tmem_slot);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
+
+    bool ok = true;
+    for (int kb = 0; kb < nkb && ok; ++kb) {
+        const int s = kb & 1;
+        // stage: A hi, mid, lo tiles, then B hi, mid, lo tiles
+        uint8_t *st = smem + s * S::stage;
+        uint8_t *a_hi = st, *b_hi = st + (EXACT ? 3 : 1) * S::a_bytes;
+        // the MMAs of K-block kb - 2 read this stage: wait (bounded) until
+        // they are done; the CTA leaves the loop together if a wait gave up
+        int waited = 1;
+        if (kb >= 2) waited = tc::mbar_wait(&bar[s], ((kb - 2) >> 1) & 1, g.err, 11) ? 1 : 0;
+        if (!__syncthreads_and(waited)) { ok = false; break; }
+        const int k0 = kbeg + kb * BK;
+        stage_operand<BM, EXACT>(g.A, g.lda, g.a_kmajor, m0, g.M, k0, kend, vec_a != 0, a_hi, S::a_bytes);
+        stage_operand<BN, EXACT>(g.B, g.ldb, g.b_kmajor, n0, g.N, k0, kend, vec_b != 0, b_hi, S::b_bytes);
+        fence_proxy_async();  // generic-proxy stores -> visible to the tensor core
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc::tc_fence_after();
+            const uint32_t ah = tc::smem_u32(a_hi), bh = tc::smem_u32(b_hi);
+#pragma unroll
+            for (int j = 0; j < BK / 16; ++j) {
+                const uint32_t o = uint32_t(j * 32);
+                tc::mma_f16(tmem, tc::smem_desc(ah + o, SWB), tc::smem_desc(bh + o, SWB), idesc,
+                            (kb > 0 || j > 0) ? 1u : 0u);
+                if (EXACT) {
+                    // (piece of A, piece of B): 0 = hi, 1 = mid, 2 = lo
+                    constexpr int pa[5] = {0, 1, 0, 1, 2}, pb[5] = {1, 0, 2, 1, 0};
+#pragma unroll
+                    for (int t = 0; t < 5; ++t)
+                        tc::mma_f16(tmem, tc::smem_desc(ah + uint32_t(pa[t] * S::a_bytes) + o, SWB),
+                                    tc::smem_desc(bh + uint32_t(pb[t] * S::b_bytes) + o, SWB), idesc, 1u);
+                }
+            }
+            tc::mma_commit(&bar[s]);
+        }
+    }
+    // the last commit (bounded wait) before the accumulator is read or freed;
+    // after a failed wait the earlier commits are waited for too
+    if (nkb > 0) {
+        const int last = nkb - 1;
+        if (!tc::mbar_wait(&bar[last & 1], (last >> 1) & 1, g.err, 12)) ok = false;
+        if (nkb > 1) tc::mbar_wait(&bar[(last - 1) & 1], ((last - 1) >> 1) & 1, g.err, 12);
+    }
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;  // CTA-uniform: the TMEM loads below are .sync.aligned
+    tc::tc_fence_after();
+    const int row = m0 + warp * 32 + lane;
+    const bool rvalid = row < g.M;
+    float *C = g.C + size_t(blockIdx.z) * size_t(g.M) * size_t(g.ldc);
+    for (int c = 0; c < BN / 32; ++c) {
+        float v[32];
+        if (nkb > 0 && ok) {
+            __syncwarp();
+            tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c * 32), v);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c * 32 + j;
+            const bool valid = rvalid && n < g.N;
+            float x = v[j];
+            if (g.bias && n < g.N) x += g.bias[n];
+            if (g.relu) x = fmaxf(x, 0.0f);
+            if (g.mask && valid && !(g.mask[int64_t(row) * g.ldc + n] > 0.0f)) x = 0.0f;
+            if (valid) C[int64_t(row) * g.ldc + n] = x;
+            if (g.colsum) {
+                float t = valid ? x : 0.0f;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                if (lane == 0) red[warp * BN + c * 32 + j] = t;
+            }
+        }
+    }
+    if (g.colsum) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < BN; t += GT)
+            if (n0 + t < g.N)
+                g.colsum[int64_t(blockIdx.x) * g.N + n0 + t] = ((red[t] + red[BN + t]) + red[2 * BN + t]) + red[3 * BN + t];
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc<BN>(tmem);
+    }
+}
+
+template <int BN, bool EXACT>
+cudaError_t launch_gemm_t(const MlpGemm &g, int vec_a, int vec_b, cudaStream_t st) {
+    const size_t smem = GemmSmem<BN, EXACT>::total;
+    auto kern = mlp_gemm_kernel<BN, EXACT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(unsigned((g.M + BM - 1) / BM), unsigned((g.N + BN - 1) / BN), unsigned(g.splits));
+    kern<<<grid, GT, smem, st>>>(g, vec_a, vec_b);
+    return cudaGetLastError();
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 // Triplet loss on Z = [anchors; positives; negatives] (3B rows of E):
 // l = max(0, |a-p|^2 - |a-n|^2 + margin), mean over the batch; writes dL/dZ.
@@ -118,27 +264,43 @@ __global__ void triplet_kernel(const float *__restrict__ Z, int B, int E, float 
     }
 }
 
-// dH *= (H > 0)
-__global__ void relu_backward_kernel(float *__restrict__ dH, const float *__restrict__ H, int64_t count) {
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
-        if (!(H[i] > 0.0f)) dH[i] = 0.0f;
+// Column sums of G (rows x N) in `parts` row ranges: out[p * N + n].  Block
+// (32 columns x 8 row lanes); the 8 lanes are combined in a fixed order.
+__global__ void colsum_parts_kernel(const float *__restrict__ G, int rows, int N, int parts, float *__restrict__ out) {
+    __shared__ float s[8][33];
+    const int n = blockIdx.x * 32 + threadIdx.x;
+    const int p = blockIdx.y;
+    const int per = (rows + parts - 1) / parts;
+    const int r0 = p * per, r1 = min(rows, r0 + per);
+    float acc = 0.0f;
+    if (n < N)
+        for (int r = r0 + int(threadIdx.y); r < r1; r += 8) acc += G[int64_t(r) * N + n];
+    s[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && n < N) {
+        float t = 0.0f;
+        for (int y = 0; y < 8; ++y) t += s[y][threadIdx.x];
+        out[int64_t(p) * N + n] = t;
+    }
 }
 
-// out[n] = sum over rows of G[row][n]
-__global__ void colsum_kernel(const float *__restrict__ G, int rows, int N, float *__restrict__ out) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    float s = 0.0f;
-    for (int r = 0; r < rows; ++r) s += G[size_t(r) * N + n];
-    out[n] = s;
+// out[i] = sum over p of G[p * count + i] (parts summed in order)
+__global__ void sum_parts_kernel(const float *__restrict__ G, int parts, int64_t count, float *__restrict__ out) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        float g = 0.0f;
+        for (int p = 0; p < parts; ++p) g += G[int64_t(p) * count + i];
+        out[i] = g;
+    }
 }
 
-__global__ void adam_kernel(float *__restrict__ W, const float *__restrict__ G, float *__restrict__ Mo,
+// Adam on W with the gradient summed from `parts` partial gradients in order.
+__global__ void adam_kernel(float *__restrict__ W, const float *__restrict__ G, int parts, float *__restrict__ Mo,
                             float *__restrict__ Vo, int64_t count, float lr, float b1, float b2, float eps,
                             float c1, float c2) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
          i += int64_t(gridDim.x) * blockDim.x) {
-        const float g = G[i];
+        float g = 0.0f;
+        for (int p = 0; p < parts; ++p) g += G[int64_t(p) * count + i];
         const float m = b1 * Mo[i] + (1.0f - b1) * g;
         const float v = b2 * Vo[i] + (1.0f - b2) * g * g;
         Mo[i] = m;
@@ -147,15 +309,33 @@ __global__ void adam_kernel(float *__restrict__ W, const float *__restrict__ G, 
     }
 }
 
+// X rows [part * bb, part * bb + bb) = S rows idx[part * T + off + i]: the
+// anchors, positives and negatives of one batch in one launch.
+__global__ void gather3_kernel(const float *__restrict__ S, const int64_t *__restrict__ idx, int64_t T, int64_t off,
+                               int bb, int d, float *__restrict__ X) {
+    const int part = blockIdx.y;
+    const int64_t total = int64_t(bb) * d;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = e / d, c = e % d;
+        X[(int64_t(part) * bb + i) * d + c] = S[idx[part * T + off + i] * d + c];
+    }
+}
+
 }  // namespace
 
-cudaError_t mlp_gemm(const float *A, const float *B, const float *bias, float *C, int M, int N, int K, int ta, int tb,
-                     int relu, int bf16, int accumulate, cudaStream_t st, int *launches) {
-    if (M <= 0 || N <= 0) return cudaSuccess;
-    dim3 grid(unsigned((N + GT - 1) / GT), unsigned((M + GT - 1) / GT));
+int mlp_gemm_mtiles(int M) { return (M + BM - 1) / BM; }
+
+cudaError_t mlp_gemm(const MlpGemm &g, cudaStream_t st, int *launches) {
+    if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+    // split-K parts are summed later: no epilogue that is not linear in them
+    if (g.splits < 1 || !g.err || (g.splits > 1 && (g.bias || g.relu || g.mask || g.colsum)))
+        return cudaErrorInvalidValue;
+    // 16-byte loads of K-major rows when every row start is 16-byte aligned
+    const int vec_a = g.a_kmajor && g.lda % 4 == 0 && aligned16(g.A);
+    const int vec_b = g.b_kmajor && g.ldb % 4 == 0 && aligned16(g.B);
     if (launches) *launches += 1;
-    mlp_gemm_kernel<<<grid, 256, 0, st>>>(A, B, bias, C, M, N, K, ta, tb, relu, bf16, accumulate);
-    return cudaGetLastError();
+    if (g.N <= 64) return g.exact ? launch_gemm_t<64, true>(g, vec_a, vec_b, st) : launch_gemm_t<64, false>(g, vec_a, vec_b, st);
+    return g.exact ? launch_gemm_t<128, true>(g, vec_a, vec_b, st) : launch_gemm_t<128, false>(g, vec_a, vec_b, st);
 }
 
 cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
@@ -165,28 +345,37 @@ cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, f
     return cudaGetLastError();
 }
 
-cudaError_t mlp_relu_backward(float *dH, const float *H, int64_t count, cudaStream_t st, int *launches) {
+cudaError_t mlp_colsum_parts(const float *G, int rows, int N, int parts, float *out, cudaStream_t st, int *launches) {
+    if (launches) *launches += 1;
+    colsum_parts_kernel<<<dim3(unsigned((N + 31) / 32), unsigned(parts)), dim3(32, 8), 0, st>>>(G, rows, N, parts, out);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_sum_parts(const float *G, int parts, int64_t count, float *out, cudaStream_t st, int *launches) {
     if (launches) *launches += 1;
     int64_t blocks = (count + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    relu_backward_kernel<<<unsigned(blocks), 256, 0, st>>>(dH, H, count);
+    sum_parts_kernel<<<unsigned(blocks), 256, 0, st>>>(G, parts, count, out);
     return cudaGetLastError();
 }
 
-cudaError_t mlp_colsum(const float *G, int rows, int N, float *out, cudaStream_t st, int *launches) {
-    if (launches) *launches += 1;
-    colsum_kernel<<<unsigned((N + 127) / 128), 128, 0, st>>>(G, rows, N, out);
-    return cudaGetLastError();
-}
-
-cudaError_t mlp_adam(float *W, const float *G, float *M, float *V, int64_t count, float lr, int step,
+cudaError_t mlp_adam(float *W, const float *G, int parts, float *M, float *V, int64_t count, float lr, int step,
                      cudaStream_t st, int *launches) {
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - powf(b1, float(step)), c2 = 1.0f - powf(b2, float(step));
     if (launches) *launches += 1;
     int64_t blocks = (count + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    adam_kernel<<<unsigned(blocks), 256, 0, st>>>(W, G, M, V, count, lr, b1, b2, 1e-8f, c1, c2);
+    adam_kernel<<<unsigned(blocks), 256, 0, st>>>(W, G, parts, M, V, count, lr, b1, b2, 1e-8f, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_gather3(const float *S, const int64_t *idx, int64_t T, int64_t off, int bb, int d, float *X,
+                        cudaStream_t st, int *launches) {
+    if (launches) *launches += 1;
+    int64_t blocks = (int64_t(bb) * d + 255) / 256;
+    if (blocks > 2048) blocks = 2048;
+    gather3_kernel<<<dim3(unsigned(blocks), 3), 256, 0, st>>>(S, idx, T, off, bb, d, X);
     return cudaGetLastError();
 }
 

@@ -44,6 +44,8 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 namespace ssg {
 
 namespace {
@@ -158,6 +160,9 @@ struct TcArgs {
     // and wraps around.  Null: identity order, no rotation.
     const uint32_t *perm;
     const int *rot;
+    // first query tile of this launch (a scan may be launched in waves of
+    // query tiles, see launch_tc_scan)
+    int64_t qt0;
 };
 
 template <int QT, int STAGES>
@@ -176,7 +181,7 @@ __device__ __forceinline__ int tc_live_warps(const TcArgs &a) {
     int live = 0;
     for (int q = 0; q < QT; ++q)
         for (int w = 0; w < 4; ++w)
-            if ((int64_t(blockIdx.x) * QT + q) * TILE + w * 32 < a.m) live += CS;
+            if ((a.qt0 + int64_t(blockIdx.x) * QT + q) * TILE + w * 32 < a.m) live += CS;
     return live;
 }
 
@@ -301,7 +306,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
     if (t_hi > a.n_tiles) t_hi = a.n_tiles;
     const int T_tiles = t_hi > t_lo ? int(t_hi - t_lo) : 0;
     // database tile of the CTA's t-th step: t_lo + t, rotated by rot[x]
-    const int64_t rot = a.rot ? int64_t(a.rot[blockIdx.x]) : 0;
+    const int64_t rot = a.rot ? int64_t(a.rot[a.qt0 + blockIdx.x]) : 0;
     auto phys_tile = [&](int t) {
         int64_t p = t_lo + t + rot;
         return p >= a.n_tiles ? p - a.n_tiles : p;
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         if (lane == 0) {
             tc::mbar_arrive_expect_tx(a_full, uint32_t(QT * tile_bytes));
             for (int q = 0; q < QT; ++q)
-                tc::bulk_g2s(sA + q * tile_bytes, a.qt + (size_t(blockIdx.x) * QT + q) * tile_bytes,
+                tc::bulk_g2s(sA + q * tile_bytes, a.qt + (size_t(a.qt0) + size_t(blockIdx.x) * QT + q) * tile_bytes,
                              uint32_t(tile_bytes), a_full);
             int issued = 0;
             for (int t = 0; t < T_tiles; ++t) {
@@ -369,7 +374,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         const int cs = (e / 4) % CS;
         const int quarter = warp % 4;
         const int row = quarter * 32 + lane;
-        const int64_t query = (int64_t(blockIdx.x) * QT + q) * TILE + row;
+        const int64_t query = (a.qt0 + int64_t(blockIdx.x) * QT + q) * TILE + row;
         constexpr int hs = QT * TILE * CS;
         constexpr int CHUNKS = TILE / 32 / CS;  // 32-column chunks per warp and tile
         // padding rows of a partial query tile filter everything out (a
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         T.fcap = a.fcap;
         T.query = query;
         if (!FILTER) Heap{T.heap, a.kk, hs}.init();
-        const bool warp_live = (int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
+        const bool warp_live = (a.qt0 + int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
             const int b = t % NACC;
             int ok = 1;
@@ -442,7 +447,9 @@ cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(unsigned((a.m + QT * TILE - 1) / (QT * TILE)), unsigned(a.splits));
-    kern<<<grid, tc_threads<QT>(), smem, st>>>(a);
+    TcArgs b = a;
+    b.qt0 = 0;
+    kern<<<grid, tc_threads<QT>(), smem, st>>>(b);
     return cudaGetLastError();
 }
 
@@ -526,7 +533,8 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
     const int64_t w_lo = int64_t(blockIdx.y) * split_w;
     const int64_t w_hi = w_lo + split_w < n_wide ? w_lo + split_w : n_wide;
     const int W = w_hi > w_lo ? int(w_hi - w_lo) : 0;
-    const int64_t rot = a.rot ? int64_t(a.rot[blockIdx.x]) / 2 : 0;
+    const int64_t qx = a.qt0 + blockIdx.x;  // query tile
+    const int64_t rot = a.rot ? int64_t(a.rot[qx]) / 2 : 0;
     auto phys_wide = [&](int u) {
         int64_t p = w_lo + u + rot;
         return p >= n_wide ? p - n_wide : p;
@@ -535,7 +543,7 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
     if (warp == 0) {
         if (lane == 0) {
             tc::mbar_arrive_expect_tx(a_full, uint32_t(tile_bytes));
-            tc::bulk_g2s(sA, a.qt + size_t(blockIdx.x) * tile_bytes, uint32_t(tile_bytes), a_full);
+            tc::bulk_g2s(sA, a.qt + size_t(qx) * tile_bytes, uint32_t(tile_bytes), a_full);
             const int steps = W * kblocks;
             int issued = 0;
             for (int st = 0; st < steps; ++st) {
@@ -589,7 +597,7 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
         const int cs = e / 4;
         const int quarter = warp % 4;
         const int row = quarter * 32 + lane;
-        const int64_t query = int64_t(blockIdx.x) * TILE + row;
+        const int64_t query = qx * TILE + row;
         constexpr int hs = TILE * CS;
         ChunkTopK<MC> T;
         T.heap = heap_base + (e * 32 + lane);
@@ -608,7 +616,7 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
         T.fcap = 0;
         T.query = query;
         Heap{T.heap, a.kk, hs}.init();
-        const bool warp_live = int64_t(blockIdx.x) * TILE + quarter * 32 < a.m;
+        const bool warp_live = qx * TILE + quarter * 32 < a.m;
         for (int u = 0; warp_live && u < W; ++u) {
             const int b = u & 1;
             int ok = 1;
@@ -659,23 +667,319 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
     }
 }
 
+// Launches the wide scan over all query tiles, `wave` query tiles per
+// launch (0: one launch).  A wave of one CTA per SM starts together, so with
+// the locality order (query tile x starting at database tile ~x) its CTAs
+// read a sliding window of neighbouring database tiles at any moment and the
+// database streams through L2 about once per wave; one launch of every tile
+// instead staggers the CTAs' start times over the whole scan.
 template <int KST, int MC>
-cudaError_t launch_wide_t(const TcArgs &a, cudaStream_t st) {
+cudaError_t launch_wide_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *launches) {
     size_t smem = WideSmem<KST>::total(a.kp, a.kk);
     if (smem < kAloneSmem) smem = kAloneSmem;  // all 512 TMEM columns: alone on the SM
     auto kern = tc_wide_kernel<KST, MC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    dim3 grid(unsigned((a.m + TILE - 1) / TILE), unsigned(a.splits));
-    kern<<<grid, tc_threads<1>(), smem, st>>>(a);
-    return cudaGetLastError();
+    const int64_t qtiles = (a.m + TILE - 1) / TILE;
+    const int64_t per = wave > 0 ? wave : qtiles;
+    for (int64_t t0 = 0; t0 < qtiles; t0 += per) {
+        TcArgs b = a;
+        b.qt0 = t0;
+        dim3 grid(unsigned(std::min<int64_t>(per, qtiles - t0)), unsigned(a.splits));
+        kern<<<grid, tc_threads<1>(), smem, st>>>(b);
+        if (launches) *launches += 1;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 template <int KST>
-cudaError_t launch_wide_mc(const TcArgs &a, int mc, cudaStream_t st) {
-    if (mc == MC_SQ) return launch_wide_t<KST, MC_SQ>(a, st);
-    if (mc == MC_COS) return launch_wide_t<KST, MC_COS>(a, st);
-    return launch_wide_t<KST, MC_DOT>(a, st);
+cudaError_t launch_wide_mc(const TcArgs &a, int mc, cudaStream_t st, int64_t wave, int *launches) {
+    if (mc == MC_SQ) return launch_wide_t<KST, MC_SQ>(a, st, wave, launches);
+    if (mc == MC_COS) return launch_wide_t<KST, MC_COS>(a, st, wave, launches);
+    return launch_wide_t<KST, MC_DOT>(a, st, wave, launches);
+}
+
+// ---------------------------------------------------------------------------
+// The pair scan: the wide scan on CTA pairs (clusters of two) with M = 256
+// MMAs (tcgen05 cta_group::2).  Each CTA owns one 128-row query tile, as in
+// the wide scan, and both CTAs of a pair scan the same database tiles; the
+// even CTA issues one 256 x 256 x 16 MMA per K step that reads the query
+// tiles of both CTAs and the database rows of both: rows 0..127 of each
+// 256-row wide tile sit in the even CTA's ring, rows 128..255 in the odd
+// one's.  So each SM loads half of every database K-block (8 KB instead of
+// 16 KB): half the L2 -> SM traffic per query, and a ring twice as deep in
+// the same shared memory to cover the copies' latency.  Each CTA's TMEM
+// holds its own 128 query rows x 256 columns, so the epilogue is the wide
+// scan's.
+//
+// Hand-offs.  Each CTA's copies complete on its own mbarriers.  The odd
+// CTA's warp 1 forwards every landed copy (its query tile, each ring stage)
+// to an mbarrier in the even CTA (pa_full, pfull[s]), where the MMA thread
+// waits for both halves.  The MMA thread's commits arrive on the barriers of
+// both CTAs (empty[s] for the producers, acc_full[b] for the epilogues).
+// The odd CTA's epilogue warps release an accumulator by arriving on the
+// even CTA's pacc_empty[b].  Every wait is bounded; both CTAs meet at a
+// cluster barrier before TMEM is freed, so no CTA leaves while the other's
+// MMAs may still read its shared memory.
+// ---------------------------------------------------------------------------
+constexpr int PKBLK = TILE * SW;  // one 128-row half of a wide K-block: 8 KB
+
+template <int KST>
+struct PairSmem {
+    static size_t total(int kp, int kk) {
+        return 1024 + size_t(TILE) * kp * 2 + size_t(KST) * PKBLK + TcSmem<1, 1>::heap_bytes(kk) + 512;
+    }
+};
+
+template <int KST, int MC>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) tc_pair_kernel(TcArgs a) {
+    constexpr int CS = 2;
+    constexpr int NACC = 2;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const size_t tile_bytes = size_t(TILE) * a.kp * 2;
+    const int kblocks = a.kp / KBE;
+    uint8_t *sA = smem;
+    uint8_t *sB = sA + tile_bytes;  // KST stages of PKBLK bytes
+    uint64_t *heap_base = reinterpret_cast<uint64_t *>(sB + size_t(KST) * PKBLK);
+    uint64_t *buf_base = heap_base + size_t(TILE) * CS * a.kk;
+    uint64_t *bars = buf_base + size_t(TILE) * CS * kBufCap;
+    uint64_t *a_full = bars;                 // this CTA's query tile landed
+    uint64_t *pa_full = a_full + 1;          // (even CTA) the odd CTA's query tile landed
+    uint64_t *full = pa_full + 1;            // this CTA's half of stage s landed
+    uint64_t *pfull = full + KST;            // (even CTA) the odd CTA's half of stage s landed
+    uint64_t *empty = pfull + KST;           // the MMAs of stage s are done
+    uint64_t *acc_full = empty + KST;        // accumulator b holds a finished wide tile
+    uint64_t *acc_empty = acc_full + NACC;   // (even CTA) its epilogue warps released b
+    uint64_t *pacc_empty = acc_empty + NACC; // (even CTA) the odd CTA's epilogue warps released b
+    uint64_t *mma_done = pacc_empty + NACC;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    const uint32_t rank = tc::cluster_ctarank();  // 0: the even CTA (issues the MMAs)
+    const uint32_t peer = rank ^ 1u;
+    const int64_t qx = a.qt0 + blockIdx.x;  // this CTA's query tile
+    const int64_t qpair = qx - int64_t(rank);
+    // live epilogue warps of a query tile: its lane quarters holding a query
+    auto live_warps = [&](int64_t tile) {
+        int live = 0;
+        for (int w = 0; w < 4; ++w)
+            if (tile * TILE + w * 32 < a.m) live += CS;
+        return live;
+    };
+    const int live_self = live_warps(qx), live_peer = live_warps(qpair + int64_t(peer));
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(a_full, 1);
+        tc::mbar_init(pa_full, 1);
+        for (int s = 0; s < KST; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&pfull[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < NACC; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], live_self > 0 ? live_self : 1);
+            tc::mbar_init(&pacc_empty[b], live_peer > 0 ? live_peer : 1);
+        }
+        tc::mbar_init(mma_done, 1);
+        tc::fence_mbarrier_init();
+    }
+    if (warp == 1) tc::tmem_alloc_pair<512>(tmem_slot);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::cluster_sync();  // both CTAs' barriers exist before any cross-CTA arrive
+    tc::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    // wide tiles and the scan order: both CTAs of a pair follow the even
+    // CTA's query tile's locality rotation
+    const int64_t n_wide = (a.n_tiles + 1) / 2;
+    const int64_t split_w = (n_wide + a.splits - 1) / a.splits;
+    const int64_t w_lo = int64_t(blockIdx.y) * split_w;
+    const int64_t w_hi = w_lo + split_w < n_wide ? w_lo + split_w : n_wide;
+    const int W = w_hi > w_lo ? int(w_hi - w_lo) : 0;
+    const int64_t rot = a.rot ? int64_t(a.rot[qpair]) / 2 : 0;
+    auto phys_wide = [&](int u) {
+        int64_t p = w_lo + u + rot;
+        return p >= n_wide ? p - n_wide : p;
+    };
+    const int steps = W * kblocks;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: this CTA's query tile, then its half of every K-block
+            tc::mbar_arrive_expect_tx(a_full, uint32_t(tile_bytes));
+            tc::bulk_g2s(sA, a.qt + size_t(qx) * tile_bytes, uint32_t(tile_bytes), a_full);
+            int issued = 0;
+            for (int st = 0; st < steps; ++st) {
+                const int s = st % KST;
+                if (!tc::mbar_wait(&empty[s], ((st / KST) & 1) ^ 1, a.err, 1)) break;
+                const int u = st / kblocks, kb = st % kblocks;
+                const uint8_t *src = a.dt + size_t(2 * phys_wide(u) + rank) * tile_bytes + size_t(kb) * KBLK;
+                tc::mbar_arrive_expect_tx(&full[s], uint32_t(PKBLK));
+                tc::bulk_g2s(sB + size_t(s) * PKBLK, src, uint32_t(PKBLK), &full[s]);
+                issued = st + 1;
+            }
+            // wait (bounded) until every copy this thread issued has landed
+            tc::mbar_wait(a_full, 0, a.err, 2);
+            for (int st = issued - KST < 0 ? 0 : issued - KST; st < issued; ++st)
+                tc::mbar_wait(&full[st % KST], (st / KST) & 1, a.err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 1) {
+            // the odd CTA forwards its landed copies to the even CTA
+            const uint32_t r_pa = tc::mapa_shared(tc::smem_u32(pa_full), peer);
+            if (tc::mbar_wait(a_full, 0, a.err, 8)) {
+                tc::mbar_arrive_cluster(r_pa);
+                for (int st = 0; st < steps; ++st) {
+                    const int s = st % KST;
+                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 9)) break;
+                    tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(&pfull[s]), peer));
+                }
+            }
+        } else if (lane == 0) {
+            // the even CTA issues the pair MMAs
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * TILE, WIDE);
+            bool ok = tc::mbar_wait(a_full, 0, a.err, 3) && tc::mbar_wait(pa_full, 0, a.err, 3);
+            const uint32_t a_addr = tc::smem_u32(sA);
+            const uint32_t b_addr0 = tc::smem_u32(sB);
+            const uint32_t r_empty0 = tc::mapa_shared(tc::smem_u32(empty), peer);
+            const uint32_t r_acc_full0 = tc::mapa_shared(tc::smem_u32(acc_full), peer);
+            for (int u = 0; ok && u < W; ++u) {
+                const int b = u & 1;
+                const uint32_t ph = ((u >> 1) & 1) ^ 1;
+                if (!tc::mbar_wait(&acc_empty[b], ph, a.err, 5)) break;
+                if (live_peer > 0 && !tc::mbar_wait(&pacc_empty[b], ph, a.err, 5)) break;
+                const uint32_t d_tmem = tmem_base + uint32_t(b * WIDE);
+                for (int kb = 0; ok && kb < kblocks; ++kb) {
+                    const int st = u * kblocks + kb;
+                    const int s = st % KST;
+                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 4) ||
+                        !tc::mbar_wait(&pfull[s], (st / KST) & 1, a.err, 4)) { ok = false; break; }
+                    tc::tc_fence_after();
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {  // two K = 16 steps per 32-element K-block
+                        const uint64_t ad = tc::smem_desc(a_addr + uint32_t(kb * KBLK + h * 32), SW);
+                        const uint64_t bd = tc::smem_desc(b_addr0 + uint32_t(s * PKBLK + h * 32), SW);
+                        tc::mma_f16_pair(d_tmem, ad, bd, idesc, (kb > 0 || h > 0) ? 1u : 0u);
+                    }
+                    tc::mma_commit_pair(tc::smem_u32(&empty[s]));
+                    tc::mma_commit_pair(r_empty0 + uint32_t(s * 8));
+                }
+                if (!ok) break;
+                tc::mma_commit_pair(tc::smem_u32(&acc_full[b]));
+                tc::mma_commit_pair(r_acc_full0 + uint32_t(b * 8));
+            }
+            tc::mma_commit_pair(tc::smem_u32(mma_done));
+            tc::mbar_wait(mma_done, 0, a.err, 6);
+        }
+        __syncwarp();
+    } else {
+        const int e = warp - 2;
+        const int cs = e / 4;
+        const int quarter = warp % 4;
+        const int row = quarter * 32 + lane;
+        const int64_t query = qx * TILE + row;
+        constexpr int hs = TILE * CS;
+        const uint32_t r_pacc0 = tc::mapa_shared(tc::smem_u32(pacc_empty), peer);
+        ChunkTopK<MC> T;
+        T.heap = heap_base + (e * 32 + lane);
+        T.cbuf = buf_base + (e * 32 + lane);
+        T.hs = hs;
+        T.kk = a.kk;
+        T.n = a.n;
+        T.perm = a.perm;
+        T.qvalid = query < a.m;
+        T.nbuf = 0;
+        T.top = KEY_EMPTY;
+        T.topd = T.qvalid ? INFINITY : -INFINITY;
+        T.ntopd = -T.topd;
+        T.fout = nullptr;
+        T.fcount = nullptr;
+        T.fcap = 0;
+        T.query = query;
+        Heap{T.heap, a.kk, hs}.init();
+        const bool warp_live = qx * TILE + quarter * 32 < a.m;
+        for (int u = 0; warp_live && u < W; ++u) {
+            const int b = u & 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&acc_full[b], (u >> 1) & 1, a.err, 7) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            tc::tc_fence_after();
+            constexpr int LDC = MC == MC_DOT ? 4 : 2;
+            const int64_t row0 = phys_wide(u) * WIDE + cs * TILE;
+            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * TILE);
+            uint32_t r[LDC][32];
+#pragma unroll
+            for (int round = 0; round < 4 / LDC; ++round) {
+                __syncwarp();
+#pragma unroll
+                for (int c = 0; c < LDC; ++c)
+                    tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
+                tc::tmem_wait_ld();
+                if (round == 4 / LDC - 1) {
+                    tc::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (rank == 0) tc::mbar_arrive(&acc_empty[b]);
+                        else tc::mbar_arrive_cluster(r_pacc0 + uint32_t(b * 8));
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+            }
+        }
+        T.top = heap_drain_raw<MC == MC_DOT>(T.heap, T.cbuf, a.kk, hs, T.nbuf, T.top, a.perm);
+        if (query < a.m) {
+            Heap H{T.heap, a.kk, hs};
+            H.sort_ascending();
+            const size_t qrow = a.perm ? size_t(a.perm[query]) : size_t(query);
+            uint64_t *out = a.cand + ((qrow * a.splits + blockIdx.y) * CS + cs) * a.kk;
+            for (int i = 0; i < a.kk; ++i) out[i] = H.h[i * hs];
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::cluster_sync();  // the even CTA's MMAs are done with both CTAs' shared memory
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc_pair<512>(tmem_base);
+    }
+}
+
+// Launches the pair scan over all query tiles (rounded up to an even count:
+// the query tile sets are allocated in pairs), `wave` query tiles per launch
+// (0: one launch; rounded up to an even count).
+template <int KST, int MC>
+cudaError_t launch_pair_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *launches) {
+    size_t smem = PairSmem<KST>::total(a.kp, a.kk);
+    if (smem < kAloneSmem) smem = kAloneSmem;  // all 512 TMEM columns: alone on the SM
+    auto kern = tc_pair_kernel<KST, MC>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    const int64_t qtiles = ((a.m + TILE - 1) / TILE + 1) / 2 * 2;
+    const int64_t per = wave > 0 ? (wave + 1) / 2 * 2 : qtiles;
+    for (int64_t t0 = 0; t0 < qtiles; t0 += per) {
+        TcArgs b = a;
+        b.qt0 = t0;
+        dim3 grid(unsigned(std::min<int64_t>(per, qtiles - t0)), unsigned(a.splits));
+        kern<<<grid, tc_threads<1>(), smem, st>>>(b);
+        if (launches) *launches += 1;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <int KST>
+cudaError_t launch_pair_mc(const TcArgs &a, int mc, cudaStream_t st, int64_t wave, int *launches) {
+    if (mc == MC_SQ) return launch_pair_t<KST, MC_SQ>(a, st, wave, launches);
+    if (mc == MC_COS) return launch_pair_t<KST, MC_COS>(a, st, wave, launches);
+    return launch_pair_t<KST, MC_DOT>(a, st, wave, launches);
 }
 
 // thr[q] = the smallest over the query's segments of the segment's last
@@ -808,6 +1112,20 @@ bool tc_wide_fits(int kp, int kk) {
     int kst = 0;
     return wide_choose(kp, kk, &kst);
 }
+bool pair_choose(int kp, int kk, int *kst);
+bool tc_pair_fits(int kp, int kk) {
+    int kst = 0;
+    return pair_choose(kp, kk, &kst);
+}
+// Ring depth of the pair scan (8 KB stages); false if fewer than four fit.
+bool pair_choose(int kp, int kk, int *kst) {
+    if (PairSmem<12>::total(kp, kk) <= kMaxSmem) { *kst = 12; return true; }
+    if (PairSmem<10>::total(kp, kk) <= kMaxSmem) { *kst = 10; return true; }
+    if (PairSmem<8>::total(kp, kk) <= kMaxSmem) { *kst = 8; return true; }
+    if (PairSmem<6>::total(kp, kk) <= kMaxSmem) { *kst = 6; return true; }
+    if (PairSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
+    return false;
+}
 bool wide_choose(int kp, int kk, int *kst) {
     if (WideSmem<5>::total(kp, kk) <= kMaxSmem) { *kst = 5; return true; }
     if (WideSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
@@ -902,7 +1220,7 @@ cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm, const int *rot,
-                           bool wide) {
+                           bool wide, int64_t wave, bool pair) {
     // (qt_out receives the query tiles per CTA; segments per split follow from it)
     TcArgs a{};
     a.qt = q_tiles;
@@ -919,18 +1237,26 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     a.err = err;
     a.perm = perm;
     a.rot = rot;
-    int qt = 1, stages = 0, kst = 0;
-    const bool use_wide = wide && wide_choose(a.kp, kk, &kst);
-    if (!use_wide && !tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
+    int qt = 1, stages = 0, kst = 0, pkst = 0;
+    const bool use_pair = wide && pair && pair_choose(a.kp, kk, &pkst);
+    const bool use_wide = !use_pair && wide && wide_choose(a.kp, kk, &kst);
+    if (!use_pair && !use_wide && !tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
     if ((perm || rot) && qt != 1) return cudaErrorInvalidValue;
     if (qt_out) *qt_out = qt;
-    if (launches) *launches += 1;
     const int mc = metric_class(metric);
-    if (use_wide) {
-        if (kst == 5) return launch_wide_mc<5>(a, mc, st);
-        if (kst == 4) return launch_wide_mc<4>(a, mc, st);
-        return launch_wide_mc<3>(a, mc, st);
+    if (use_pair) {
+        if (pkst == 12) return launch_pair_mc<12>(a, mc, st, wave, launches);
+        if (pkst == 10) return launch_pair_mc<10>(a, mc, st, wave, launches);
+        if (pkst == 8) return launch_pair_mc<8>(a, mc, st, wave, launches);
+        if (pkst == 6) return launch_pair_mc<6>(a, mc, st, wave, launches);
+        return launch_pair_mc<4>(a, mc, st, wave, launches);
     }
+    if (use_wide) {
+        if (kst == 5) return launch_wide_mc<5>(a, mc, st, wave, launches);
+        if (kst == 4) return launch_wide_mc<4>(a, mc, st, wave, launches);
+        return launch_wide_mc<3>(a, mc, st, wave, launches);
+    }
+    if (launches) *launches += 1;
     if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
     if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
     return launch_tc_mc<1, 2>(a, mc, st);

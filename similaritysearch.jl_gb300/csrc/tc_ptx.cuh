@@ -211,5 +211,70 @@ __host__ __device__ __forceinline__ uint32_t swizzled_offset(uint32_t r, uint32_
     return off ^ (((off >> 7) & mask) << 4);
 }
 
+// ---- CTA pairs (cluster of two, tcgen05 cta_group::2) ----------------------
+// A pair MMA (M = 256) is issued by the even CTA of a cluster of two and
+// reads the A and B operands of both CTAs at the same shared-memory offsets:
+// rows 0..127 of A and of B from the even CTA, rows 128..255 from the odd
+// one; each CTA's TMEM receives its own 128 rows of D.  A kernel that uses
+// cta_group::2 uses it for every tcgen05 allocation, MMA and commit.
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Shared::cluster address of the same shared variable in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t smem_addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_addr), "r"(rank));
+    return r;
+}
+
+// Arrives once on an mbarrier of another CTA of the cluster (release at
+// cluster scope: the arriving thread's prior shared-memory reads and TMEM
+// loads are ordered before it).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+// Every thread of both CTAs of the cluster.
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// One warp of each CTA of the pair: the same NCOLS columns in both CTAs' TMEM.
+template <int NCOLS>
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t *dst_smem) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+                 "n"(NCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "n"(NCOLS) : "memory");
+}
+
+// D[tmem of both CTAs] (+)= A * B^T over the pair, kind::f16, M = 256.
+__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                             uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrives once on the mbarrier at `cluster_addr` (this CTA's or the peer's)
+// when the pair MMAs this thread issued so far have completed.
+__device__ __forceinline__ void mma_commit_pair(uint32_t cluster_addr) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(cluster_addr)
+                 : "memory");
+}
+
 }  // namespace tc
 }  // namespace ssg

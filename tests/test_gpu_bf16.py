@@ -172,6 +172,41 @@ def test_bf16_wide_equals_narrow(ss, d, k, name):
     assert O.macrorecall(fi, gi) >= 0.97
 
 
+@pytest.mark.parametrize("name,d,k,m,splits", [("normcosine", 96, 32, 300, 0), ("sql2", 64, 10, 129, 3),
+                                                ("cosine", 128, 20, 1000, 0), ("ip", 32, 5, 1, 0),
+                                                ("sql2", 256, 8, 385, 2)])
+def test_bf16_pair_scan_equals_single_cta_scan(ss, name, d, k, m, splits):
+    # the pair scan (CTA pairs, M = 256 MMAs, each CTA loading half of every
+    # database K-block) keeps exactly the candidates of the one-CTA wide
+    # scan: odd query-tile counts (the last pair's second tile is padding),
+    # forced database splits, one query
+    rng = np.random.default_rng(d + k + m)
+    X = mixture(rng, 12000, d, normalise=(name in ("normcosine", "cosine")))
+    Q = X[rng.integers(0, 12000, size=m)] + rng.standard_normal((m, d), dtype=np.float32) * 0.02
+    if name == "normcosine":
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    pi, pd = run(ss, name, X, Q, k, overfetch=1.5, pair=1, splits=splits)
+    wi, wd = run(ss, name, X, Q, k, overfetch=1.5, pair=0, splits=splits)
+    assert np.array_equal(pi, wi) and np.array_equal(pd, wd)
+    check_reported_distances_exact(name, X, Q, pi[:8], pd[:8])
+
+
+@pytest.mark.parametrize("name", ["normcosine", "sql2"])
+def test_bf16_pair_scan_allknn_locality_identical(ss, name):
+    # allknn over 313 query tiles (odd) in the locality order on CTA pairs
+    # equals the one-CTA scan, self excluded
+    rng = np.random.default_rng(17 + len(name))
+    n, d = 40000, 96
+    X = mixture(rng, n, d, centres=300, normalise=(name != "sql2"))
+    X[700:800] = X[:100]
+    dist = getattr(ss.Dist, NAMES[name])()
+    idx = ss.GPUExhaustiveSearch(dist, ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.5)
+    ids_p, dists_p = ss.allknn(idx, ss.GenericContext(), 32, exclude_self=True)
+    idx.set_param("pair", 0)
+    ids_w, dists_w = ss.allknn(idx, ss.GenericContext(), 32, exclude_self=True)
+    assert np.array_equal(ids_p, ids_w) and np.array_equal(dists_p, dists_w)
+
+
 def test_bf16_autotune_scan_keeps_results(ss):
     # the autotuner times scan shapes (tile width, database splits); every
     # shape keeps the same candidates, so the tuned index answers exactly as
