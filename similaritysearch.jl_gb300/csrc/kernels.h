@@ -235,15 +235,24 @@ struct MlpGemm {
 };
 cudaError_t mlp_gemm(const MlpGemm &g, cudaStream_t st, int *launches);
 int mlp_gemm_mtiles(int M);  // M tiles = rows of the column-sum partials
+int mlp_gemm_ntiles(int N);  // N tiles of a product with N columns
+// K splits giving about `want` CTAs for a product of `ctas` output tiles (at
+// most one split per 64-element K-block, the K-blocks spread evenly)
+int mlp_splits(int K, int ctas, int want);
+// C (M x N) = sum of the `parts` split products P[p] (M x N each) + bias[n],
+// ReLU, column sums per 128 rows (colsum[tile * N + n], optional)
+cudaError_t mlp_reduce_parts(const float *P, int parts, int M, int N, const float *bias, int relu, float *C,
+                             float *colsum, cudaStream_t st, int *launches);
 cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
                         cudaStream_t st, int *launches);
 // out[p * N + n] = sum of G[r][n] over the p-th of `parts` row ranges
 cudaError_t mlp_colsum_parts(const float *G, int rows, int N, int parts, float *out, cudaStream_t st, int *launches);
 // out[i] = sum over p < parts of G[p * count + i]
 cudaError_t mlp_sum_parts(const float *G, int parts, int64_t count, float *out, cudaStream_t st, int *launches);
-// Adam step on W; the gradient is the sum of `parts` partials G[p * count + i]
-cudaError_t mlp_adam(float *W, const float *G, int parts, float *M, float *V, int64_t count, float lr, int step,
-                     cudaStream_t st, int *launches);
+// Adam steps on four parameter groups in one launch (group g: W[g], its
+// gradient summed from parts[g] partials of count[g] entries, moments M, V)
+cudaError_t mlp_adam4(float *const W[4], const float *const G[4], const int parts[4], float *const M[4],
+                      float *const V[4], const int64_t count[4], float lr, int step, cudaStream_t st, int *launches);
 // X = [S[idx[off..]]; S[idx[T + off..]]; S[idx[2T + off..]]] (bb rows each)
 cudaError_t mlp_gather3(const float *S, const int64_t *idx, int64_t T, int64_t off, int bb, int d, float *X,
                         cudaStream_t st, int *launches);

@@ -351,26 +351,34 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
         cudaMemcpy(d_trip, trip.data(), trip.size() * 8, cudaMemcpyHostToDevice);
         // 4. training buffers.  One step: X = the batch's anchors, positives
         // and negatives (3B rows), H = relu(X W1^T + b1), Z = H W2^T + b2,
-        // the loss and dZ, gW2 = dZ^T H (split K), dH = (dZ W2) * (H > 0)
-        // with its per-tile column sums (gb1), gW1 = dH^T X (split K), the
-        // column sums of dZ (gb2), then Adam summing each gradient's parts in
-        // a fixed order.  All products on the tensor cores (mlp.cu).
+        // the loss and dZ, gW2 = dZ^T H, dH = (dZ W2) * (H > 0) with its
+        // per-tile column sums (gb1), gW1 = dH^T X, the column sums of dZ
+        // (gb2), then Adam summing each gradient's parts in a fixed order.
+        // Every product runs on the tensor cores (mlp.cu) split along K so
+        // that each CTA walks about two K-blocks (the products are small:
+        // one CTA per output tile would serialise a global-load round trip
+        // per K-block); the forward products' parts are summed by a reduction
+        // that applies the bias and the ReLU.
         const int B = t.batch;
         const int R = 3 * B;
         const int mt = mlp_gemm_mtiles(R);                 // row tiles: parts of gb1
-        const int s1 = std::max(1, std::min(16, R / 384)); // K splits of gW1 (M = H, N = d)
-        const int s2 = std::max(1, std::min(16, R / 256)); // K splits of gW2 (M = E, N = H)
+        const int kWant = 2 * device_sm_count();           // CTAs per product
+        const int sf1 = mlp_splits(int(d), mt * mlp_gemm_ntiles(int(H)), kWant);
+        const int sf2 = mlp_splits(int(H), mt * mlp_gemm_ntiles(int(E)), kWant);
+        const int s1 = mlp_splits(R, mlp_gemm_mtiles(int(H)) * mlp_gemm_ntiles(int(d)), kWant);
+        const int s2 = mlp_splits(R, mlp_gemm_mtiles(int(E)) * mlp_gemm_ntiles(int(H)), kWant);
         const int pb2 = std::max(1, std::min(32, R / 96)); // row ranges of gb2's column sums
         float *X = dmalloc(size_t(R) * d, cu, "x"), *Hh = dmalloc(size_t(R) * H, cu, "h"), *Z = dmalloc(size_t(R) * E, cu, "z");
         float *dZ = dmalloc(size_t(R) * E, cu, "dz"), *dH = dmalloc(size_t(R) * H, cu, "dh");
+        float *P = dmalloc(std::max(size_t(sf1) * R * H, size_t(sf2) * R * E), cu, "parts");
         float *gW1 = dmalloc(size_t(s1) * H * d, cu, "g"), *gb1 = dmalloc(size_t(mt) * H, cu, "g");
         float *gW2 = dmalloc(size_t(s2) * E * H, cu, "g"), *gb2 = dmalloc(size_t(pb2) * E, cu, "g");
         const size_t npar = size_t(H) * d + H + size_t(E) * H + E;
         float *mom = dmalloc(2 * npar, cu, "adam");
         float *stat = dmalloc(2, cu, "loss");
         int *ew = err_word(m, cu);
-        if (!X || !Hh || !Z || !dZ || !dH || !gW1 || !gb1 || !gW2 || !gb2 || !mom || !stat || !ew) {
-            for (float *p : {X, Hh, Z, dZ, dH, gW1, gb1, gW2, gb2, mom, stat})
+        if (!X || !Hh || !Z || !dZ || !dH || !P || !gW1 || !gb1 || !gW2 || !gb2 || !mom || !stat || !ew) {
+            for (float *p : {X, Hh, Z, dZ, dH, P, gW1, gb1, gW2, gb2, mom, stat})
                 if (p) cudaFree(p);
             cudaFree(S); cudaFree(d_trip);
             return fail(SSG_ENOMEM);
@@ -389,36 +397,41 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
                 ++step;
                 MlpGemm f1, f2, gw2, dh, gw1;
                 f1.err = f2.err = gw2.err = dh.err = gw1.err = ew;
-                // H = relu(X W1^T + b1)
-                f1.A = X; f1.lda = d; f1.B = m->W1; f1.ldb = d; f1.C = Hh; f1.ldc = H;
-                f1.M = rows; f1.N = int(H); f1.K = int(d); f1.bias = m->b1; f1.relu = 1;
-                // Z = H W2^T + b2
-                f2.A = Hh; f2.lda = H; f2.B = m->W2; f2.ldb = H; f2.C = Z; f2.ldc = E;
-                f2.M = rows; f2.N = int(E); f2.K = int(H); f2.bias = m->b2;
+                // parts of X W1^T, then H = relu(sum + b1)
+                f1.A = X; f1.lda = d; f1.B = m->W1; f1.ldb = d; f1.C = P; f1.ldc = H;
+                f1.M = rows; f1.N = int(H); f1.K = int(d); f1.splits = sf1;
+                // parts of H W2^T, then Z = sum + b2
+                f2.A = Hh; f2.lda = H; f2.B = m->W2; f2.ldb = H; f2.C = P; f2.ldc = E;
+                f2.M = rows; f2.N = int(E); f2.K = int(H); f2.splits = sf2;
                 // gW2 (E x H) = dZ^T H: both operands transposed, K = rows
                 gw2.A = dZ; gw2.lda = E; gw2.a_kmajor = 0; gw2.B = Hh; gw2.ldb = H; gw2.b_kmajor = 0;
                 gw2.C = gW2; gw2.ldc = H; gw2.M = int(E); gw2.N = int(H); gw2.K = rows; gw2.splits = s2;
-                // dH = (dZ W2) * (H > 0), column sums per row tile (gb1)
+                // dH = (dZ W2) * (H > 0), column sums per row tile (gb1); K = E
                 dh.A = dZ; dh.lda = E; dh.B = m->W2; dh.ldb = H; dh.b_kmajor = 0; dh.C = dH; dh.ldc = H;
                 dh.M = rows; dh.N = int(H); dh.K = int(E); dh.mask = Hh; dh.colsum = gb1;
                 // gW1 (H x d) = dH^T X, K = rows
                 gw1.A = dH; gw1.lda = H; gw1.a_kmajor = 0; gw1.B = X; gw1.ldb = d; gw1.b_kmajor = 0;
                 gw1.C = gW1; gw1.ldc = d; gw1.M = int(H); gw1.N = int(d); gw1.K = rows; gw1.splits = s1;
                 const int mt_b = mlp_gemm_mtiles(rows);
+                float *const aw[4] = {m->W1, m->b1, m->W2, m->b2};
+                const float *const ag[4] = {gW1, gb1, gW2, gb2};
+                const int ap[4] = {s1, mt_b, s2, pb2};
+                float *const am[4] = {mW1, mb1, mW2, mb2};
+                float *const av[4] = {vW1, vb1, vW2, vb2};
+                const int64_t ac[4] = {int64_t(H) * d, H, int64_t(E) * H, E};
                 bool ok = cu.ok(mlp_gather3(S, d_trip, T, off, bb, int(d), X, v.stream, v.launches), "gathering a batch") &&
                           cu.ok(cudaMemsetAsync(stat, 0, 8, v.stream), "loss") &&
                           cu.ok(mlp_gemm(f1, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_reduce_parts(P, sf1, rows, int(H), m->b1, 1, Hh, nullptr, v.stream, v.launches), "fwd") &&
                           cu.ok(mlp_gemm(f2, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_reduce_parts(P, sf2, rows, int(E), m->b2, 0, Z, nullptr, v.stream, v.launches), "fwd") &&
                           cu.ok(mlp_triplet(Z, bb, int(E), t.margin, dZ, stat, reinterpret_cast<int *>(stat + 1),
                                             v.stream, v.launches), "loss") &&
                           cu.ok(mlp_gemm(gw2, v.stream, v.launches), "bwd") &&
                           cu.ok(mlp_colsum_parts(dZ, rows, int(E), pb2, gb2, v.stream, v.launches), "bwd") &&
                           cu.ok(mlp_gemm(dh, v.stream, v.launches), "bwd") &&
                           cu.ok(mlp_gemm(gw1, v.stream, v.launches), "bwd") &&
-                          cu.ok(mlp_adam(m->W1, gW1, s1, mW1, vW1, int64_t(H) * d, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->b1, gb1, mt_b, mb1, vb1, H, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->W2, gW2, s2, mW2, vW2, int64_t(E) * H, t.lr, int(step), v.stream, v.launches), "adam") &&
-                          cu.ok(mlp_adam(m->b2, gb2, pb2, mb2, vb2, E, t.lr, int(step), v.stream, v.launches), "adam");
+                          cu.ok(mlp_adam4(aw, ag, ap, am, av, ac, t.lr, int(step), v.stream, v.launches), "adam");
                 if (!ok) status = SSG_ECUDA;
                 if (ok && (s + 1 == steps_per_epoch)) {
                     float loss = 0.0f;
@@ -431,7 +444,7 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
             }
         }
         m->train_steps = step;
-        for (float *p : {X, Hh, Z, dZ, dH, gW1, gb1, gW2, gb2, mom, stat, S}) cudaFree(p);
+        for (float *p : {X, Hh, Z, dZ, dH, P, gW1, gb1, gW2, gb2, mom, stat, S}) cudaFree(p);
         cudaFree(d_trip);
         if (status) return fail(status);
     }
@@ -519,7 +532,11 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
     Cuda cu;
     const int R = 3 * B;
     const int mt = mlp_gemm_mtiles(R);
-    const int s1 = std::max(1, std::min(16, R / 384)), s2 = std::max(1, std::min(16, R / 256));
+    const int kWant = 2 * device_sm_count();
+    const int sf1 = mlp_splits(int(d), mt * mlp_gemm_ntiles(int(H)), kWant);
+    const int sf2 = mlp_splits(int(H), mt * mlp_gemm_ntiles(int(E)), kWant);
+    const int s1 = mlp_splits(R, mlp_gemm_mtiles(int(H)) * mlp_gemm_ntiles(int(d)), kWant);
+    const int s2 = mlp_splits(R, mlp_gemm_mtiles(int(E)) * mlp_gemm_ntiles(int(H)), kWant);
     const int pb2 = std::max(1, std::min(32, R / 96));
     std::vector<void *> bufs;
     auto up = [&](const float *h, size_t n) -> float * {
@@ -535,13 +552,14 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
     float *dW1 = up(W1, size_t(H) * d), *db1 = up(b1, H), *dW2 = up(W2, size_t(E) * H), *db2 = up(b2, E);
     float *dX = up(X, size_t(R) * d), *Hh = mk(size_t(R) * H), *Z = mk(size_t(R) * E), *dZ = mk(size_t(R) * E);
     float *dH = mk(size_t(R) * H), *p1 = mk(size_t(s1) * H * d), *pb1 = mk(size_t(mt) * H), *p2 = mk(size_t(s2) * E * H);
+    float *pf = mk(std::max(size_t(sf1) * R * H, size_t(sf2) * R * E));
     float *pb2d = mk(size_t(pb2) * E), *g1 = mk(size_t(H) * d), *gb1d = mk(H), *g2 = mk(size_t(E) * H);
     float *gb2d = mk(E), *stat = mk(2);
     int *ew = reinterpret_cast<int *>(mk(1));
     int rc = SSG_OK;
     for (void *p : {(void *)dW1, (void *)db1, (void *)dW2, (void *)db2, (void *)dX, (void *)Hh, (void *)Z, (void *)dZ,
-                    (void *)dH, (void *)p1, (void *)pb1, (void *)p2, (void *)pb2d, (void *)g1, (void *)gb1d, (void *)g2,
-                    (void *)gb2d, (void *)stat, (void *)ew})
+                    (void *)dH, (void *)p1, (void *)pb1, (void *)p2, (void *)pf, (void *)pb2d, (void *)g1, (void *)gb1d,
+                    (void *)g2, (void *)gb2d, (void *)stat, (void *)ew})
         if (!p) rc = SSG_ENOMEM;
     cudaStream_t st = nullptr;
     if (!rc) {
@@ -550,17 +568,20 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
         MlpGemm f1, f2, gw2, dh, gw1;
         f1.err = f2.err = gw2.err = dh.err = gw1.err = ew;
         f1.exact = f2.exact = gw2.exact = dh.exact = gw1.exact = 1;
-        f1.A = dX; f1.lda = d; f1.B = dW1; f1.ldb = d; f1.C = Hh; f1.ldc = H;
-        f1.M = R; f1.N = int(H); f1.K = int(d); f1.bias = db1; f1.relu = 1;
-        f2.A = Hh; f2.lda = H; f2.B = dW2; f2.ldb = H; f2.C = Z; f2.ldc = E;
-        f2.M = R; f2.N = int(E); f2.K = int(H); f2.bias = db2;
+        f1.A = dX; f1.lda = d; f1.B = dW1; f1.ldb = d; f1.C = pf; f1.ldc = H;
+        f1.M = R; f1.N = int(H); f1.K = int(d); f1.splits = sf1;
+        f2.A = Hh; f2.lda = H; f2.B = dW2; f2.ldb = H; f2.C = pf; f2.ldc = E;
+        f2.M = R; f2.N = int(E); f2.K = int(H); f2.splits = sf2;
         gw2.A = dZ; gw2.lda = E; gw2.a_kmajor = 0; gw2.B = Hh; gw2.ldb = H; gw2.b_kmajor = 0;
         gw2.C = p2; gw2.ldc = H; gw2.M = int(E); gw2.N = int(H); gw2.K = R; gw2.splits = s2;
         dh.A = dZ; dh.lda = E; dh.B = dW2; dh.ldb = H; dh.b_kmajor = 0; dh.C = dH; dh.ldc = H;
         dh.M = R; dh.N = int(H); dh.K = int(E); dh.mask = Hh; dh.colsum = pb1;
         gw1.A = dH; gw1.lda = H; gw1.a_kmajor = 0; gw1.B = dX; gw1.ldb = d; gw1.b_kmajor = 0;
         gw1.C = p1; gw1.ldc = d; gw1.M = int(H); gw1.N = int(d); gw1.K = R; gw1.splits = s1;
-        bool ok = cu.ok(mlp_gemm(f1, st, nullptr), "fwd") && cu.ok(mlp_gemm(f2, st, nullptr), "fwd") &&
+        bool ok = cu.ok(mlp_gemm(f1, st, nullptr), "fwd") &&
+                  cu.ok(mlp_reduce_parts(pf, sf1, R, int(H), db1, 1, Hh, nullptr, st, nullptr), "fwd") &&
+                  cu.ok(mlp_gemm(f2, st, nullptr), "fwd") &&
+                  cu.ok(mlp_reduce_parts(pf, sf2, R, int(E), db2, 0, Z, nullptr, st, nullptr), "fwd") &&
                   cu.ok(mlp_triplet(Z, B, int(E), margin, dZ, stat, reinterpret_cast<int *>(stat + 1), st, nullptr), "loss") &&
                   cu.ok(mlp_gemm(gw2, st, nullptr), "bwd") &&
                   cu.ok(mlp_colsum_parts(dZ, R, int(E), pb2, pb2d, st, nullptr), "bwd") &&

@@ -13,8 +13,10 @@
 // reads the accumulator with tcgen05.ld and applies what the caller fused
 // in: bias, ReLU, a ReLU-derivative mask, and per-tile column sums (the bias
 // gradients, reduced in a fixed order later, so training is deterministic).
-// Weight gradients (K = the batch's 3B rows) split K across CTAs; each split
-// writes its own partial product and Adam sums the parts in order.
+// The products are small, so each is split along K over enough CTAs that
+// every CTA walks about two K-blocks; each split writes its own partial
+// product, summed in a fixed order by a reduction kernel that applies the
+// bias and ReLU (forward products) or by Adam (weight gradients).
 //
 // `exact` mode: each operand element x is split into three BF16 pieces,
 // hi = bf16(x), mid = bf16(x - hi), lo = bf16(x - hi - mid) (24 significant
@@ -53,35 +55,54 @@ __device__ __forceinline__ void fence_proxy_async() {
 // BF16 tile (hi) and, in exact mode, the tiles of its second and third
 // pieces (mid, lo) at `piece` bytes after it.  kmajor: element (r, k) at
 // X[r * ld + k], else at X[k * ld + r].  Out-of-range elements are 0.
-template <int R, bool EXACT>
-__device__ __forceinline__ void stage_operand(const float *__restrict__ X, int64_t ld, int kmajor, int r0, int rlim,
-                                              int k0, int klim, bool vec4, uint8_t *hi, int piece) {
-    constexpr int CHUNKS = R * (BK / 8);  // 16-byte chunks of 8 BF16
-    for (int c = threadIdx.x; c < CHUNKS; c += GT) {
+// Two phases: every load of the thread's chunks is issued first (registers),
+// then they are converted and stored, so a K-block costs about one global
+// load latency instead of one per chunk.
+template <int R>
+struct Staged {
+    static constexpr int CPT = R * (BK / 8) / GT;  // 16-byte chunks per thread
+    float v[CPT][8];
+};
+
+template <int R>
+__device__ __forceinline__ void load_operand(Staged<R> &t, const float *__restrict__ X, int64_t ld, int kmajor, int r0,
+                                             int rlim, int k0, int klim, bool vec4) {
+#pragma unroll
+    for (int i = 0; i < Staged<R>::CPT; ++i) {
+        const int c = int(threadIdx.x) + i * GT;
         int r, kc;
         if (kmajor) { r = c / (BK / 8); kc = c % (BK / 8); }
         else { kc = c / R; r = c % R; }  // consecutive threads: consecutive rows (coalesced)
         const int gr = r0 + r, gk = k0 + kc * 8;
-        float v[8];
-        if (gr < rlim) {
-            if (kmajor) {
-                const float *p = X + int64_t(gr) * ld + gk;
-                if (vec4 && gk + 8 <= klim) {
-                    const float4 a = *reinterpret_cast<const float4 *>(p);
-                    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
-                    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-                } else {
+        float *v = t.v[i];
+        if (gr < rlim && kmajor && vec4 && gk + 8 <= klim) {
+            const float *p = X + int64_t(gr) * ld + gk;
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(p + 4));
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        } else if (gr < rlim && kmajor) {
+            const float *p = X + int64_t(gr) * ld + gk;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? p[j] : 0.0f;
-                }
-            } else {
+            for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? __ldg(p + j) : 0.0f;
+        } else if (gr < rlim) {
 #pragma unroll
-                for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? X[int64_t(gk + j) * ld + gr] : 0.0f;
-            }
+            for (int j = 0; j < 8; ++j) v[j] = gk + j < klim ? __ldg(X + int64_t(gk + j) * ld + gr) : 0.0f;
         } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j) v[j] = 0.0f;
         }
+    }
+}
+
+template <int R, bool EXACT>
+__device__ __forceinline__ void store_operand(const Staged<R> &t, int kmajor, uint8_t *hi, int piece) {
+#pragma unroll
+    for (int i = 0; i < Staged<R>::CPT; ++i) {
+        const int c = int(threadIdx.x) + i * GT;
+        int r, kc;
+        if (kmajor) { r = c / (BK / 8); kc = c % (BK / 8); }
+        else { kc = c / R; r = c % R; }
+        const float *v = t.v[i];
         __align__(16) __nv_bfloat16 h[8];
         __align__(16) __nv_bfloat16 md[8];
         __align__(16) __nv_bfloat16 l[8];
@@ -142,8 +163,14 @@ __global__ void __launch_bounds__(GT, 1) mlp_gemm_kernel(MlpGemm g, int vec_a, i
         if (kb >= 2) waited = tc::mbar_wait(&bar[s], ((kb - 2) >> 1) & 1, g.err, 11) ? 1 : 0;
         if (!__syncthreads_and(waited)) { ok = false; break; }
         const int k0 = kbeg + kb * BK;
-        stage_operand<BM, EXACT>(g.A, g.lda, g.a_kmajor, m0, g.M, k0, kend, vec_a != 0, a_hi, S::a_bytes);
-        stage_operand<BN, EXACT>(g.B, g.ldb, g.b_kmajor, n0, g.N, k0, kend, vec_b != 0, b_hi, S::b_bytes);
+        {
+            Staged<BM> ta;
+            Staged<BN> tb;
+            load_operand<BM>(ta, g.A, g.lda, g.a_kmajor, m0, g.M, k0, kend, vec_a != 0);
+            load_operand<BN>(tb, g.B, g.ldb, g.b_kmajor, n0, g.N, k0, kend, vec_b != 0);
+            store_operand<BM, EXACT>(ta, g.a_kmajor, a_hi, S::a_bytes);
+            store_operand<BN, EXACT>(tb, g.b_kmajor, b_hi, S::b_bytes);
+        }
         fence_proxy_async();  // generic-proxy stores -> visible to the tensor core
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -233,34 +260,72 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 // Triplet loss on Z = [anchors; positives; negatives] (3B rows of E):
 // l = max(0, |a-p|^2 - |a-n|^2 + margin), mean over the batch; writes dL/dZ.
+// One warp per triplet, lanes over the embedding's coordinates.
 __global__ void triplet_kernel(const float *__restrict__ Z, int B, int E, float margin, float *__restrict__ dZ,
                                float *__restrict__ loss_sum, int *__restrict__ active) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32);
+    const int lane = threadIdx.x % 32;
     if (b >= B) return;
     const float *za = Z + size_t(b) * E;
     const float *zp = Z + size_t(B + b) * E;
     const float *zn = Z + size_t(2 * B + b) * E;
     float dp = 0.0f, dn = 0.0f;
-    for (int e = 0; e < E; ++e) {
+    for (int e = lane; e < E; e += 32) {
         const float u = za[e] - zp[e], w = za[e] - zn[e];
         dp = fmaf(u, u, dp);
         dn = fmaf(w, w, dn);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dp += __shfl_xor_sync(0xffffffffu, dp, o);
+        dn += __shfl_xor_sync(0xffffffffu, dn, o);
     }
     const float l = dp - dn + margin;
     float *ga = dZ + size_t(b) * E;
     float *gp = dZ + size_t(B + b) * E;
     float *gn = dZ + size_t(2 * B + b) * E;
     const float s = 2.0f / float(B);
-    if (l > 0.0f) {
+    const bool act = l > 0.0f;
+    if (act && lane == 0) {
         atomicAdd(loss_sum, l / float(B));
         atomicAdd(active, 1);
-        for (int e = 0; e < E; ++e) {
-            ga[e] = s * (zn[e] - zp[e]);
-            gp[e] = -s * (za[e] - zp[e]);
-            gn[e] = s * (za[e] - zn[e]);
+    }
+    for (int e = lane; e < E; e += 32) {
+        ga[e] = act ? s * (zn[e] - zp[e]) : 0.0f;
+        gp[e] = act ? -s * (za[e] - zp[e]) : 0.0f;
+        gn[e] = act ? s * (za[e] - zn[e]) : 0.0f;
+    }
+}
+
+// C[m][n] = epilogue(sum over p of P[p][m][n]) for the split-K products:
+// + bias[n], ReLU, column sums per block of 128 rows (colsum[blockIdx.x][n]).
+// Block = 32 columns x 8 row lanes over 128 rows; parts and row lanes are
+// summed in a fixed order (deterministic).
+__global__ void reduce_parts_kernel(const float *__restrict__ P, int parts, int M, int N, const float *__restrict__ bias,
+                                    int relu, float *__restrict__ C, float *__restrict__ colsum) {
+    __shared__ float s[8][33];
+    const int n = blockIdx.y * 32 + threadIdx.x;
+    const int r0 = blockIdx.x * 128;
+    const int64_t stride = int64_t(M) * N;
+    float acc = 0.0f;
+    if (n < N) {
+        const float b = bias ? bias[n] : 0.0f;
+        for (int r = r0 + int(threadIdx.y); r < min(M, r0 + 128); r += 8) {
+            float v = 0.0f;
+            for (int p = 0; p < parts; ++p) v += P[p * stride + int64_t(r) * N + n];
+            v += b;
+            if (relu) v = fmaxf(v, 0.0f);
+            C[int64_t(r) * N + n] = v;
+            acc += v;
         }
-    } else {
-        for (int e = 0; e < E; ++e) { ga[e] = 0.0f; gp[e] = 0.0f; gn[e] = 0.0f; }
+    }
+    if (!colsum) return;
+    s[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && n < N) {
+        float t = 0.0f;
+        for (int y = 0; y < 8; ++y) t += s[y][threadIdx.x];
+        colsum[int64_t(blockIdx.x) * N + n] = t;
     }
 }
 
@@ -293,37 +358,75 @@ __global__ void sum_parts_kernel(const float *__restrict__ G, int parts, int64_t
     }
 }
 
-// Adam on W with the gradient summed from `parts` partial gradients in order.
-__global__ void adam_kernel(float *__restrict__ W, const float *__restrict__ G, int parts, float *__restrict__ Mo,
-                            float *__restrict__ Vo, int64_t count, float lr, float b1, float b2, float eps,
-                            float c1, float c2) {
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
-         i += int64_t(gridDim.x) * blockDim.x) {
-        float g = 0.0f;
-        for (int p = 0; p < parts; ++p) g += G[int64_t(p) * count + i];
-        const float m = b1 * Mo[i] + (1.0f - b1) * g;
-        const float v = b2 * Vo[i] + (1.0f - b2) * g * g;
+// X rows [part * bb, part * bb + bb) = S rows idx[part * T + off + i]: the
+// anchors, positives and negatives of one batch in one launch, one block per
+// row (16-byte copies when the rows allow them).
+__global__ void gather3_kernel(const float *__restrict__ S, const int64_t *__restrict__ idx, int64_t T, int64_t off,
+                               int bb, int d, float *__restrict__ X) {
+    const int part = blockIdx.y;
+    const int i = blockIdx.x;
+    const float *src = S + idx[part * T + off + i] * d;
+    float *dst = X + (int64_t(part) * bb + i) * d;
+    if ((d & 3) == 0) {
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+        for (int c = threadIdx.x; c < d / 4; c += blockDim.x) d4[c] = __ldg(s4 + c);
+    } else {
+        for (int c = threadIdx.x; c < d; c += blockDim.x) dst[c] = __ldg(src + c);
+    }
+}
+
+// Adam on up to four parameter groups in one launch (blockIdx.y = group);
+// each gradient is the sum of its `parts` partials, taken in order.
+struct AdamGroups {
+    float *W[4];
+    const float *G[4];
+    float *M[4], *V[4];
+    int64_t count[4];
+    int parts[4];
+};
+
+__global__ void adam_groups_kernel(AdamGroups a, float lr, float b1, float b2, float eps, float c1, float c2) {
+    const int g = blockIdx.y;
+    float *__restrict__ W = a.W[g];
+    const float *__restrict__ G = a.G[g];
+    float *__restrict__ Mo = a.M[g];
+    float *__restrict__ Vo = a.V[g];
+    const int64_t count = a.count[g];
+    const int parts = a.parts[g];
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        float gr = 0.0f;
+        for (int p = 0; p < parts; ++p) gr += G[int64_t(p) * count + i];
+        const float m = b1 * Mo[i] + (1.0f - b1) * gr;
+        const float v = b2 * Vo[i] + (1.0f - b2) * gr * gr;
         Mo[i] = m;
         Vo[i] = v;
         W[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
     }
 }
 
-// X rows [part * bb, part * bb + bb) = S rows idx[part * T + off + i]: the
-// anchors, positives and negatives of one batch in one launch.
-__global__ void gather3_kernel(const float *__restrict__ S, const int64_t *__restrict__ idx, int64_t T, int64_t off,
-                               int bb, int d, float *__restrict__ X) {
-    const int part = blockIdx.y;
-    const int64_t total = int64_t(bb) * d;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t i = e / d, c = e % d;
-        X[(int64_t(part) * bb + i) * d + c] = S[idx[part * T + off + i] * d + c];
-    }
-}
-
 }  // namespace
 
 int mlp_gemm_mtiles(int M) { return (M + BM - 1) / BM; }
+int mlp_gemm_ntiles(int N) { return N <= 64 ? 1 : (N + 127) / 128; }
+
+int mlp_splits(int K, int ctas, int want) {
+    const int kblocks = (K + BK - 1) / BK;
+    int s = (want + ctas - 1) / ctas;
+    s = s < 1 ? 1 : s;
+    s = s > kblocks ? kblocks : s;
+    const int per = (kblocks + s - 1) / s;  // K-blocks per split, then as few splits as that needs
+    return (kblocks + per - 1) / per;
+}
+
+cudaError_t mlp_reduce_parts(const float *P, int parts, int M, int N, const float *bias, int relu, float *C,
+                             float *colsum, cudaStream_t st, int *launches) {
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    if (launches) *launches += 1;
+    reduce_parts_kernel<<<dim3(unsigned((M + 127) / 128), unsigned((N + 31) / 32)), dim3(32, 8), 0, st>>>(
+        P, parts, M, N, bias, relu, C, colsum);
+    return cudaGetLastError();
+}
 
 cudaError_t mlp_gemm(const MlpGemm &g, cudaStream_t st, int *launches) {
     if (g.M <= 0 || g.N <= 0) return cudaSuccess;
@@ -341,7 +444,7 @@ cudaError_t mlp_gemm(const MlpGemm &g, cudaStream_t st, int *launches) {
 cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
                         cudaStream_t st, int *launches) {
     if (launches) *launches += 1;
-    triplet_kernel<<<unsigned((B + 127) / 128), 128, 0, st>>>(Z, B, E, margin, dZ, loss_sum, active);
+    triplet_kernel<<<unsigned((B + 7) / 8), 256, 0, st>>>(Z, B, E, margin, dZ, loss_sum, active);
     return cudaGetLastError();
 }
 
@@ -359,23 +462,29 @@ cudaError_t mlp_sum_parts(const float *G, int parts, int64_t count, float *out, 
     return cudaGetLastError();
 }
 
-cudaError_t mlp_adam(float *W, const float *G, int parts, float *M, float *V, int64_t count, float lr, int step,
-                     cudaStream_t st, int *launches) {
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.0f - powf(b1, float(step)), c2 = 1.0f - powf(b2, float(step));
+cudaError_t mlp_gather3(const float *S, const int64_t *idx, int64_t T, int64_t off, int bb, int d, float *X,
+                        cudaStream_t st, int *launches) {
+    if (bb <= 0) return cudaSuccess;
     if (launches) *launches += 1;
-    int64_t blocks = (count + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
-    adam_kernel<<<unsigned(blocks), 256, 0, st>>>(W, G, parts, M, V, count, lr, b1, b2, 1e-8f, c1, c2);
+    const int threads = d >= 512 ? 192 : 64;
+    gather3_kernel<<<dim3(unsigned(bb), 3), threads, 0, st>>>(S, idx, T, off, bb, d, X);
     return cudaGetLastError();
 }
 
-cudaError_t mlp_gather3(const float *S, const int64_t *idx, int64_t T, int64_t off, int bb, int d, float *X,
-                        cudaStream_t st, int *launches) {
+cudaError_t mlp_adam4(float *const W[4], const float *const G[4], const int parts[4], float *const M[4],
+                      float *const V[4], const int64_t count[4], float lr, int step, cudaStream_t st, int *launches) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - powf(b1, float(step)), c2 = 1.0f - powf(b2, float(step));
+    AdamGroups a{};
+    int64_t most = 1;
+    for (int g = 0; g < 4; ++g) {
+        a.W[g] = W[g]; a.G[g] = G[g]; a.M[g] = M[g]; a.V[g] = V[g]; a.count[g] = count[g]; a.parts[g] = parts[g];
+        most = count[g] > most ? count[g] : most;
+    }
+    int64_t blocks = (most + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
     if (launches) *launches += 1;
-    int64_t blocks = (int64_t(bb) * d + 255) / 256;
-    if (blocks > 2048) blocks = 2048;
-    gather3_kernel<<<dim3(unsigned(blocks), 3), 256, 0, st>>>(S, idx, T, off, bb, d, X);
+    adam_groups_kernel<<<dim3(unsigned(blocks), 4), 256, 0, st>>>(a, lr, b1, b2, 1e-8f, c1, c2);
     return cudaGetLastError();
 }
 
