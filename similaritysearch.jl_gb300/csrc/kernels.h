@@ -239,10 +239,9 @@ int mlp_gemm_ntiles(int N);  // N tiles of a product with N columns
 // K splits giving about `want` CTAs for a product of `ctas` output tiles (at
 // most one split per 64-element K-block, the K-blocks spread evenly)
 int mlp_splits(int K, int ctas, int want);
-// C (M x N) = sum of the `parts` split products P[p] (M x N each) + bias[n],
-// ReLU, column sums per 128 rows (colsum[tile * N + n], optional)
+// C (M x N) = sum of the `parts` split products P[p] (M x N each) + bias[n], ReLU
 cudaError_t mlp_reduce_parts(const float *P, int parts, int M, int N, const float *bias, int relu, float *C,
-                             float *colsum, cudaStream_t st, int *launches);
+                             cudaStream_t st, int *launches);
 cudaError_t mlp_triplet(const float *Z, int B, int E, float margin, float *dZ, float *loss_sum, int *active,
                         cudaStream_t st, int *launches);
 // out[p * N + n] = sum of G[r][n] over the p-th of `parts` row ranges

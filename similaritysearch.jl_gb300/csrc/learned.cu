@@ -422,9 +422,9 @@ int learned_train(const IndexView &v, const TrainArgs &t, LearnedModel **out, st
                 bool ok = cu.ok(mlp_gather3(S, d_trip, T, off, bb, int(d), X, v.stream, v.launches), "gathering a batch") &&
                           cu.ok(cudaMemsetAsync(stat, 0, 8, v.stream), "loss") &&
                           cu.ok(mlp_gemm(f1, v.stream, v.launches), "fwd") &&
-                          cu.ok(mlp_reduce_parts(P, sf1, rows, int(H), m->b1, 1, Hh, nullptr, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_reduce_parts(P, sf1, rows, int(H), m->b1, 1, Hh, v.stream, v.launches), "fwd") &&
                           cu.ok(mlp_gemm(f2, v.stream, v.launches), "fwd") &&
-                          cu.ok(mlp_reduce_parts(P, sf2, rows, int(E), m->b2, 0, Z, nullptr, v.stream, v.launches), "fwd") &&
+                          cu.ok(mlp_reduce_parts(P, sf2, rows, int(E), m->b2, 0, Z, v.stream, v.launches), "fwd") &&
                           cu.ok(mlp_triplet(Z, bb, int(E), t.margin, dZ, stat, reinterpret_cast<int *>(stat + 1),
                                             v.stream, v.launches), "loss") &&
                           cu.ok(mlp_gemm(gw2, v.stream, v.launches), "bwd") &&
@@ -579,9 +579,9 @@ int learned_grad_check(int64_t d, int64_t H, int64_t E, const float *W1, const f
         gw1.A = dH; gw1.lda = H; gw1.a_kmajor = 0; gw1.B = dX; gw1.ldb = d; gw1.b_kmajor = 0;
         gw1.C = p1; gw1.ldc = d; gw1.M = int(H); gw1.N = int(d); gw1.K = R; gw1.splits = s1;
         bool ok = cu.ok(mlp_gemm(f1, st, nullptr), "fwd") &&
-                  cu.ok(mlp_reduce_parts(pf, sf1, R, int(H), db1, 1, Hh, nullptr, st, nullptr), "fwd") &&
+                  cu.ok(mlp_reduce_parts(pf, sf1, R, int(H), db1, 1, Hh, st, nullptr), "fwd") &&
                   cu.ok(mlp_gemm(f2, st, nullptr), "fwd") &&
-                  cu.ok(mlp_reduce_parts(pf, sf2, R, int(E), db2, 0, Z, nullptr, st, nullptr), "fwd") &&
+                  cu.ok(mlp_reduce_parts(pf, sf2, R, int(E), db2, 0, Z, st, nullptr), "fwd") &&
                   cu.ok(mlp_triplet(Z, B, int(E), margin, dZ, stat, reinterpret_cast<int *>(stat + 1), st, nullptr), "loss") &&
                   cu.ok(mlp_gemm(gw2, st, nullptr), "bwd") &&
                   cu.ok(mlp_colsum_parts(dZ, R, int(E), pb2, pb2d, st, nullptr), "bwd") &&

@@ -10,7 +10,8 @@
 // K-contiguously or, for a transposed operand, M-contiguously (coalesced
 // either way), while one thread issues the MMAs of the previous K-block: two
 // stages, an mbarrier per stage signalled by tcgen05.commit.  The epilogue
-// reads the accumulator with tcgen05.ld and applies what the caller fused
+// reads the accumulator with tcgen05.ld, turns each 32 x 32 block through
+// shared memory (coalesced row writes) and applies what the caller fused
 // in: bias, ReLU, a ReLU-derivative mask, and per-tile column sums (the bias
 // gradients, reduced in a fixed order later, so training is deterministic).
 // The products are small, so each is split along K over enough CTAs that
@@ -202,8 +203,12 @@ __global__ void __launch_bounds__(GT, 1) mlp_gemm_kernel(MlpGemm g, int vec_a, i
     }
     ok = __syncthreads_and(ok ? 1 : 0) != 0;  // CTA-uniform: the TMEM loads below are .sync.aligned
     tc::tc_fence_after();
-    const int row = m0 + warp * 32 + lane;
-    const bool rvalid = row < g.M;
+    // Each warp's 32 x 32 blocks pass through shared memory (the operand
+    // stages are free once the last commit has arrived) so that a lane
+    // writes one column and a store instruction covers 32 consecutive
+    // columns of one row; the bias, ReLU, mask and column sums are applied in
+    // that pass, where each lane owns one column.
+    float *tile = reinterpret_cast<float *>(smem) + warp * (32 * 33);
     float *C = g.C + size_t(blockIdx.z) * size_t(g.M) * size_t(g.ldc);
     for (int c = 0; c < BN / 32; ++c) {
         float v[32];
@@ -215,21 +220,25 @@ __global__ void __launch_bounds__(GT, 1) mlp_gemm_kernel(MlpGemm g, int vec_a, i
             for (int j = 0; j < 32; ++j) v[j] = 0.0f;
         }
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int n = n0 + c * 32 + j;
-            const bool valid = rvalid && n < g.N;
-            float x = v[j];
-            if (g.bias && n < g.N) x += g.bias[n];
+        for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = v[j];  // row = lane
+        __syncwarp();
+        const int n = n0 + c * 32 + lane;
+        const bool nvalid = n < g.N;
+        const float b = (g.bias && nvalid) ? g.bias[n] : 0.0f;
+        float csum = 0.0f;
+        for (int r = 0; r < 32; ++r) {
+            const int row = m0 + warp * 32 + r;
+            const bool valid = nvalid && row < g.M;
+            float x = tile[r * 33 + lane] + b;
             if (g.relu) x = fmaxf(x, 0.0f);
             if (g.mask && valid && !(g.mask[int64_t(row) * g.ldc + n] > 0.0f)) x = 0.0f;
-            if (valid) C[int64_t(row) * g.ldc + n] = x;
-            if (g.colsum) {
-                float t = valid ? x : 0.0f;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-                if (lane == 0) red[warp * BN + c * 32 + j] = t;
+            if (valid) {
+                C[int64_t(row) * g.ldc + n] = x;
+                csum += x;
             }
         }
+        if (g.colsum) red[warp * BN + c * 32 + lane] = csum;
+        __syncwarp();
     }
     if (g.colsum) {
         __syncthreads();
@@ -297,35 +306,26 @@ __global__ void triplet_kernel(const float *__restrict__ Z, int B, int E, float 
     }
 }
 
-// C[m][n] = epilogue(sum over p of P[p][m][n]) for the split-K products:
-// + bias[n], ReLU, column sums per block of 128 rows (colsum[blockIdx.x][n]).
-// Block = 32 columns x 8 row lanes over 128 rows; parts and row lanes are
-// summed in a fixed order (deterministic).
+// C[m][n] = sum over p of P[p][m][n] (in order) + bias[n], ReLU: the
+// epilogue of the split-K forward products.  Block = 32 columns x 8 rows,
+// each thread four rows 8 apart.
 __global__ void reduce_parts_kernel(const float *__restrict__ P, int parts, int M, int N, const float *__restrict__ bias,
-                                    int relu, float *__restrict__ C, float *__restrict__ colsum) {
-    __shared__ float s[8][33];
+                                    int relu, float *__restrict__ C) {
     const int n = blockIdx.y * 32 + threadIdx.x;
-    const int r0 = blockIdx.x * 128;
+    if (n >= N) return;
     const int64_t stride = int64_t(M) * N;
-    float acc = 0.0f;
-    if (n < N) {
-        const float b = bias ? bias[n] : 0.0f;
-        for (int r = r0 + int(threadIdx.y); r < min(M, r0 + 128); r += 8) {
-            float v = 0.0f;
-            for (int p = 0; p < parts; ++p) v += P[p * stride + int64_t(r) * N + n];
-            v += b;
-            if (relu) v = fmaxf(v, 0.0f);
-            C[int64_t(r) * N + n] = v;
-            acc += v;
-        }
-    }
-    if (!colsum) return;
-    s[threadIdx.y][threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.y == 0 && n < N) {
-        float t = 0.0f;
-        for (int y = 0; y < 8; ++y) t += s[y][threadIdx.x];
-        colsum[int64_t(blockIdx.x) * N + n] = t;
+    const float b = bias ? bias[n] : 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = blockIdx.x * 32 + i * 8 + int(threadIdx.y);
+        if (r >= M) break;
+        const float *src = P + int64_t(r) * N + n;
+        float v = 0.0f;
+#pragma unroll 4
+        for (int p = 0; p < parts; ++p) v += src[p * stride];
+        v += b;
+        if (relu) v = fmaxf(v, 0.0f);
+        C[int64_t(r) * N + n] = v;
     }
 }
 
@@ -420,11 +420,11 @@ int mlp_splits(int K, int ctas, int want) {
 }
 
 cudaError_t mlp_reduce_parts(const float *P, int parts, int M, int N, const float *bias, int relu, float *C,
-                             float *colsum, cudaStream_t st, int *launches) {
+                             cudaStream_t st, int *launches) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     if (launches) *launches += 1;
-    reduce_parts_kernel<<<dim3(unsigned((M + 127) / 128), unsigned((N + 31) / 32)), dim3(32, 8), 0, st>>>(
-        P, parts, M, N, bias, relu, C, colsum);
+    reduce_parts_kernel<<<dim3(unsigned((M + 31) / 32), unsigned((N + 31) / 32)), dim3(32, 8), 0, st>>>(
+        P, parts, M, N, bias, relu, C);
     return cudaGetLastError();
 }
 
