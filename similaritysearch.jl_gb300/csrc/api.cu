@@ -102,6 +102,7 @@ struct ssg_index {
     // tiles of every smp_r-th database row, filtered lists, counts, bounds
     DevBuf tc_smp, tc_smp_norm, f_out, f_cnt, f_thr, gbound;
     DevBuf pack_q, pack_out;  // ssg_search_batches staging
+    DevBuf qbound;            // per-query bounds shared by a query's split heaps (ScanArgs::qbound)
     // plain GEMM-form scan: k-major tiles of the database (built for gm_rows
     // rows) and of the current queries
     DevBuf gm_db, gm_q;
@@ -488,6 +489,12 @@ int run_exact_scan(ssg_index *idx, const void *dq, const float *dqn, int64_t m, 
         a.cand = static_cast<uint64_t *>(cand.p);
         a.id_base = 0;
         const void *qc = static_cast<const char *>(dq) + size_t(c0) * qrow_bytes;
+        if (splits > 1) {
+            // the splits of a query share one bound (all ones: none yet)
+            SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
+            SSG_CK(cudaMemsetAsync(idx->qbound.p, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
+            a.qbound = static_cast<uint32_t *>(idx->qbound.p);
+        }
         size_t gh = idx->metric == SSG_METRIC_HAMMING ? ssg::hamming_gheap_bytes(a) : ssg::direct_gheap_bytes(a);
         if (gh) {
             SSG_CK(idx->gheap.ensure(gh), "allocating heap scratch");
@@ -590,6 +597,12 @@ int run_gemm(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k
         a.cand = static_cast<uint64_t *>(idx->cand.p);
         const float *qc = dq + size_t(c0) * idx->dim;
         const float *xaux = sq ? static_cast<const float *>(idx->sq_norm.p) : static_cast<const float *>(idx->db_norm.p);
+        if (splits > 1) {
+            // the splits of a query share one bound (all ones: none yet)
+            SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
+            SSG_CK(cudaMemsetAsync(idx->qbound.p, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
+            a.qbound = static_cast<uint32_t *>(idx->qbound.p);
+        }
         SSG_RC(timer.begin());
         SSG_CK(ssg::launch_gemm_f32(a, static_cast<const float *>(idx->gm_db.p), xaux,
                                     qtile_base + size_t(c0 / 128) * ssg::gemm_tile_floats(idx->dim),
@@ -836,13 +849,20 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
                "building BF16 query tiles");
         qtiles = static_cast<const uint8_t *>(idx->tc_q.p);
     }
+    // the splits of a query share one bound (all ones: none yet)
+    uint32_t *qbound = nullptr;
+    if (splits > 1) {
+        SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
+        qbound = static_cast<uint32_t *>(idx->qbound.p);
+    }
     for (int64_t c0 = 0; c0 < m; c0 += chunk) {
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        if (qbound) SSG_CK(cudaMemsetAsync(qbound, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
         SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, idx->dim,
                                    kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
                                    static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
-                                   perm, rot, idx->wide_param != 0, idx->wave_param, idx->pair_param != 0),
+                                   perm, rot, idx->wide_param != 0, idx->wave_param, idx->pair_param != 0, qbound),
                "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
@@ -1259,7 +1279,7 @@ std::vector<uint64_t> graph_key(const ssg_index *idx, int64_t m, int k) {
     for (const DevBuf *b : {&idx->db, &idx->db_norm, &idx->tc_db, &idx->tc_norm, &idx->tc_q, &idx->st_db,
                             &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale, &idx->cand,
                             &idx->red[0], &idx->red[1], &idx->status, &idx->gbound, &idx->qnorm, &idx->pack_q,
-                            &idx->pack_out})
+                            &idx->pack_out, &idx->qbound})
         key.push_back(uint64_t(reinterpret_cast<uintptr_t>(b->p)));
     return key;
 }

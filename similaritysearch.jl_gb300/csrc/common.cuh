@@ -234,6 +234,14 @@ __device__ __forceinline__ void block_bitonic_sort(uint64_t *s, int P) {
     __syncthreads();
 }
 
+// The shared per-query bound (see ScanArgs::qbound): lowered to `d` by one
+// heap, read back by all.
+__device__ __forceinline__ void bound_lower(uint32_t *qb, float d) { atomicMin(qb, float_to_ordered(d)); }
+__device__ __forceinline__ float bound_read(const uint32_t *qb) {
+    const uint32_t u = __ldcg(qb);
+    return u == 0xffffffffu ? INFINITY : ordered_to_float(u);
+}
+
 inline int next_pow2(int64_t v) {
     int p = 1;
     while (p < v) p <<= 1;

@@ -66,6 +66,9 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
     BufferedTopK T;
     T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
     const float qnorm = (METRIC == COSINE && qvalid) ? qn[qi] : 1.0f;
+    // the query's bound shared with the other splits (ScanArgs::qbound)
+    uint32_t *qb = (a.qbound && qvalid) ? a.qbound + qi : nullptr;
+    float published = INFINITY;
 
     for (int64_t j0 = lo; j0 < hi; j0 += TN) {
         float acc[TN];
@@ -109,6 +112,8 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
                 }
             }
         }
+        const float bnd = qb ? bound_read(qb) : INFINITY;
+        float thr = fminf(T.topd, bnd);
 #pragma unroll
         for (int g = 0; g < TN; g += 8) {
 #pragma unroll
@@ -116,10 +121,15 @@ direct_f32_kernel(ScanArgs a, const float *__restrict__ db, const float *__restr
                 const int64_t id = j0 + j;
                 if (qvalid && id < hi) {
                     const float d = finish<METRIC>(acc[j], METRIC == COSINE ? xn[id] : 1.0f, qnorm);
-                    if (d <= T.topd) T.append(d, uint32_t(id + a.id_base));
+                    if (d <= thr) T.append(d, uint32_t(id + a.id_base));
                 }
             }
             T.maybe_drain(kDrainTrigger);
+            thr = fminf(T.topd, bnd);
+        }
+        if (qb && T.topd < published) {
+            bound_lower(qb, T.topd);
+            published = T.topd;
         }
     }
     T.drain();

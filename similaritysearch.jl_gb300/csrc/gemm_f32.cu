@@ -216,6 +216,9 @@ gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const fl
     const bool row_valid = owner && q0 + tid < a.m;
     BufferedTopK T;
     if (owner) T.init(heaps + tid, bufs + tid, a.kk, BM);
+    // the query's bound shared with the other splits (ScanArgs::qbound)
+    uint32_t *qb = (a.qbound && row_valid) ? a.qbound + q0 + tid : nullptr;
+    float published = INFINITY;
 
     for (int64_t j0 = lo; j0 < hi; j0 += BN) {
         float acc[8][8];
@@ -254,6 +257,8 @@ gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const fl
             // warps 2h and 2h+1 own rows [64h, 64h + 64)
             if ((tid >> 6) == h) {
                 const float *row = sT + (tid - h * 64) * SROW;
+                const float bnd = qb ? bound_read(qb) : INFINITY;
+                float thr = row_valid ? fminf(T.topd, bnd) : -INFINITY;
                 // a group of 8 values is only looked at when one of the warp's
                 // rows may take one of them (padding rows take none)
 #pragma unroll 2
@@ -261,14 +266,19 @@ gemm_f32_kernel(ScanArgs a, int kpad, const float *__restrict__ dtiles, const fl
                     const float4 v0 = *reinterpret_cast<const float4 *>(row + c);
                     const float4 v1 = *reinterpret_cast<const float4 *>(row + c + 4);
                     const float gm = fmin3(fmin3(v0.x, v0.y, v0.z), fmin3(v0.w, v1.x, v1.y), fminf(v1.z, v1.w));
-                    if (!__any_sync(0xffffffffu, gm <= (row_valid ? T.topd : -INFINITY))) continue;
+                    if (!__any_sync(0xffffffffu, gm <= thr)) continue;
                     const float vv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const int64_t id = j0 + c + j;
-                        if (row_valid && vv[j] <= T.topd && id < hi) T.append(vv[j], uint32_t(id + a.id_base));
+                        if (row_valid && vv[j] <= thr && id < hi) T.append(vv[j], uint32_t(id + a.id_base));
                     }
                     T.maybe_drain(kDrainTrigger);
+                    if (row_valid) thr = fminf(T.topd, bnd);
+                }
+                if (qb && T.topd < published) {
+                    bound_lower(qb, T.topd);
+                    published = T.topd;
                 }
             }
         }

@@ -89,6 +89,9 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
 
     BufferedTopK T;
     T.init(hbase + t, hbase + size_t(a.kk) * QPB + t, a.kk, QPB);
+    // the query's bound shared with the other splits (ScanArgs::qbound)
+    uint32_t *qb = (a.qbound && qvalid) ? a.qbound + qi : nullptr;
+    float published = INFINITY;
 
     if (lo < hi) load_sketches<WMAX, QPB, VEC16>(xbuf, db, lo, hi, W);
     for (int64_t j0 = lo, it = 0; j0 < hi; j0 += TN, ++it) {
@@ -102,6 +105,8 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
         __syncthreads();
         uint64_t(*xs)[WMAX] = xbuf + (it & 1) * TN;
         const int jn = hi - j0 < TN ? int(hi - j0) : TN;
+        const float bnd = qb ? bound_read(qb) : INFINITY;
+        float thr = qvalid ? fminf(T.topd, bnd) : -INFINITY;
         for (int g = 0; g < jn; g += 8) {
             // eight rows at once: eight independent XOR + POPC chains per
             // thread (rows past the end are zero words, filtered below)
@@ -119,13 +124,18 @@ hamming_kernel(ScanArgs a, const uint64_t *__restrict__ db, const uint64_t *__re
             int dmin = d[0];
 #pragma unroll
             for (int jj = 1; jj < 8; ++jj) dmin = min(dmin, d[jj]);
-            if (!__any_sync(0xffffffffu, qvalid && float(dmin) <= T.topd)) continue;
+            if (!__any_sync(0xffffffffu, float(dmin) <= thr)) continue;
 #pragma unroll
             for (int jj = 0; jj < 8; ++jj) {
                 const float fd = float(d[jj]);
-                if (qvalid && g + jj < jn && fd <= T.topd) T.append(fd, uint32_t(j0 + g + jj + a.id_base));
+                if (qvalid && g + jj < jn && fd <= thr) T.append(fd, uint32_t(j0 + g + jj + a.id_base));
             }
             T.maybe_drain(kDrainTrigger);
+            if (qvalid) thr = fminf(T.topd, bnd);
+        }
+        if (qb && T.topd < published) {
+            bound_lower(qb, T.topd);
+            published = T.topd;
         }
         __syncthreads();  // this buffer is refilled two tiles later
     }

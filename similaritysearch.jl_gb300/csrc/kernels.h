@@ -22,6 +22,12 @@ struct ScanArgs {
     uint64_t *cand;    // m * splits * kk keys
     uint64_t *gheap;   // global heap storage when kk is too large for shared memory
     int64_t id_base;   // added to every 0-based row id in the keys
+    // optional per-query bound shared by all splits (float_to_ordered of a
+    // distance, all ones = none yet): every heap that holds kk keys lowers it
+    // to its frontier, and every heap filters against it -- any heap's kk-th
+    // key bounds the query's kk-th key over all splits, so the merged
+    // candidates do not change
+    uint32_t *qbound = nullptr;
 };
 
 // Exact FP32 scan: difference form for SqL2/L2, sequential-FMA dot for the
@@ -123,11 +129,14 @@ cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t di
 // database tile rot[x], keys carry ids and each query's candidates go to
 // the row of its id.  wave > 0: the wide scan is launched `wave` query tiles
 // at a time.  pair (with wide): the scan runs on CTA pairs with M = 256 MMAs
-// (the query tile set must then hold an even number of tiles).
+// (the query tile set must then hold an even number of tiles).  qbound: m
+// words set to all ones, the per-query bound every heap of a query shares
+// (see ScanArgs::qbound).
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm = nullptr,
-                           const int *rot = nullptr, bool wide = false, int64_t wave = 0, bool pair = false);
+                           const int *rot = nullptr, bool wide = false, int64_t wave = 0, bool pair = false,
+                           uint32_t *qbound = nullptr);
 // Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
 // segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
 // grouped by pivot) and rot (start tile of each query tile's scan).

@@ -225,13 +225,21 @@ __global__ void __launch_bounds__(GT, 1) mlp_gemm_kernel(MlpGemm g, int vec_a, i
         const int n = n0 + c * 32 + lane;
         const bool nvalid = n < g.N;
         const float b = (g.bias && nvalid) ? g.bias[n] : 0.0f;
+        // the mask values first (independent loads in flight together)
+        float mk[32];
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            const int row = m0 + warp * 32 + r;
+            mk[r] = (g.mask && nvalid && row < g.M) ? __ldg(g.mask + int64_t(row) * g.ldc + n) : 1.0f;
+        }
         float csum = 0.0f;
+#pragma unroll
         for (int r = 0; r < 32; ++r) {
             const int row = m0 + warp * 32 + r;
             const bool valid = nvalid && row < g.M;
             float x = tile[r * 33 + lane] + b;
             if (g.relu) x = fmaxf(x, 0.0f);
-            if (g.mask && valid && !(g.mask[int64_t(row) * g.ldc + n] > 0.0f)) x = 0.0f;
+            if (!(mk[r] > 0.0f)) x = 0.0f;
             if (valid) {
                 C[int64_t(row) * g.ldc + n] = x;
                 csum += x;

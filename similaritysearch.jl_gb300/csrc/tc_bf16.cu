@@ -163,6 +163,9 @@ struct TcArgs {
     // first query tile of this launch (a scan may be launched in waves of
     // query tiles, see launch_tc_scan)
     int64_t qt0;
+    // heap mode: per-query bound shared by every heap of the query (all
+    // splits and column halves), indexed by query position; null: none
+    uint32_t *qbound;
 };
 
 template <int QT, int STAGES>
@@ -209,6 +212,26 @@ struct ChunkTopK {
     int *fcount;
     int fcap;
     int64_t query;
+    // the query's shared bound (heap mode): the filter threshold is the
+    // smaller of this heap's frontier and the bound; a full heap lowers the
+    // bound to its frontier
+    uint32_t *qb;
+    float bnd, published;
+
+    __device__ __forceinline__ void set_threshold(float heap_frontier) {
+        topd = !qvalid ? -INFINITY : fminf(heap_frontier, bnd);
+        ntopd = -topd;
+        if (qb && qvalid && heap_frontier < published) {
+            bound_lower(qb, heap_frontier);
+            published = heap_frontier;
+        }
+    }
+    // once per database tile: pick up the bound the other heaps published
+    __device__ __forceinline__ void refresh() {
+        if (!qb || !qvalid) return;
+        bnd = bound_read(qb);
+        if (bnd < topd) { topd = bnd; ntopd = -bnd; }
+    }
 
     __device__ __forceinline__ void chunk(const uint32_t (&r)[32], int64_t id0, const float *__restrict__ dnorm) {
         const float *nrm = dnorm + id0;
@@ -249,8 +272,7 @@ struct ChunkTopK {
                 if (__any_sync(0xffffffffu, nbuf >= kDrainTrigger)) {
                     top = heap_drain_raw<MC == MC_DOT>(heap, cbuf, kk, hs, nbuf, top, perm);
                     nbuf = 0;
-                    topd = !qvalid ? -INFINITY : (top == KEY_EMPTY) ? INFINITY : key_dist(top);
-                    ntopd = -topd;
+                    set_threshold(top == KEY_EMPTY ? INFINITY : key_dist(top));
                 }
             }
         }
@@ -396,6 +418,9 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
         T.fcount = a.fcount;
         T.fcap = a.fcap;
         T.query = query;
+        T.qb = (!FILTER && a.qbound && T.qvalid) ? a.qbound + query : nullptr;
+        T.bnd = INFINITY;
+        T.published = INFINITY;
         if (!FILTER) Heap{T.heap, a.kk, hs}.init();
         const bool warp_live = (a.qt0 + int64_t(blockIdx.x) * QT + q) * TILE + quarter * 32 < a.m;
         for (int t = 0; warp_live && t < T_tiles; ++t) {
@@ -405,6 +430,7 @@ __global__ void __launch_bounds__(tc_threads<QT>(), 1) tc_scan_kernel(TcArgs a) 
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
+            T.refresh();
             const int64_t row0 = phys_tile(t) * TILE + cs * (TILE / CS);
             // this warp's columns in flight together, one wait, then the
             // accumulator goes back to the MMA warp before any filtering
@@ -615,6 +641,9 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
         T.fcount = nullptr;
         T.fcap = 0;
         T.query = query;
+        T.qb = (a.qbound && T.qvalid) ? a.qbound + query : nullptr;
+        T.bnd = INFINITY;
+        T.published = INFINITY;
         Heap{T.heap, a.kk, hs}.init();
         const bool warp_live = qx * TILE + quarter * 32 < a.m;
         for (int u = 0; warp_live && u < W; ++u) {
@@ -624,6 +653,7 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
+            T.refresh();
             // this warp's 128 columns, LDC 32-column loads in flight per
             // round; the accumulator goes back to the MMA warp as soon as the
             // last load landed (two accumulators only: the MMAs must not wait
@@ -901,6 +931,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
         T.fcount = nullptr;
         T.fcap = 0;
         T.query = query;
+        T.qb = (a.qbound && T.qvalid) ? a.qbound + query : nullptr;
+        T.bnd = INFINITY;
+        T.published = INFINITY;
         Heap{T.heap, a.kk, hs}.init();
         const bool warp_live = qx * TILE + quarter * 32 < a.m;
         for (int u = 0; warp_live && u < W; ++u) {
@@ -910,6 +943,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             tc::tc_fence_after();
+            T.refresh();
             constexpr int LDC = MC == MC_DOT ? 4 : 2;
             const int64_t row0 = phys_wide(u) * WIDE + cs * TILE;
             const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * TILE);
@@ -1220,7 +1254,7 @@ cudaError_t launch_filter_select(const uint64_t *fout, const int *fcount, int64_
 cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
                            int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm, const int *rot,
-                           bool wide, int64_t wave, bool pair) {
+                           bool wide, int64_t wave, bool pair, uint32_t *qbound) {
     // (qt_out receives the query tiles per CTA; segments per split follow from it)
     TcArgs a{};
     a.qt = q_tiles;
@@ -1237,6 +1271,7 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     a.err = err;
     a.perm = perm;
     a.rot = rot;
+    a.qbound = qbound;
     int qt = 1, stages = 0, kst = 0, pkst = 0;
     const bool use_pair = wide && pair && pair_choose(a.kp, kk, &pkst);
     const bool use_wide = !use_pair && wide && wide_choose(a.kp, kk, &kst);
