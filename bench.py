@@ -59,10 +59,11 @@ N_DB = 1_000_000
 DIM = 96
 K = 32
 OVERFETCH_LADDER = (1.25, 1.5, 1.75)
-# DRAM bytes (read + write) of one headline scan launch at n = 1e6, from the
-# one-metric ncu capture summarised in profiles/tc_wide_bf16_allknn.md
-HEADLINE_SCAN_TRAFFIC = 630.12e9 + 0.684e9
-HEADLINE_TRAFFIC_OVERFETCH = 1.25
+# DRAM bytes (read + write) of one headline scan launch at n = 1e6 and
+# over-fetch 1.5, from the one-pass ncu capture summarised in
+# profiles/tc_wide_bf16_allknn.md
+HEADLINE_SCAN_TRAFFIC = 579.23e9 + 0.821e9
+HEADLINE_TRAFFIC_OVERFETCH = 1.5
 
 METRIC = "queries/s @ recall@10>=0.99 (allknn NormCosine n=1e6 d=96 k=32 excl. self)"
 DATA = ("synthetic: seeded 1000-cluster Gaussian mixture (centres N(0,1), sigma U[0.1,0.5]), "
@@ -171,6 +172,16 @@ def roofline_flops(mode, flops_per_launch, avg_launch_ms):
     return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "traffic": None, "kernel": "scan", "per_launch_ms": avg_launch_ms,
             "flops_per_launch": flops_per_launch, "peak_note": note}
+
+
+def plain_tc_roofline(pairs, d, avg_launch_ms):
+    """Roofline of the plain method's scan on the tensor cores: the two-piece
+    BF16 products run over K = 3 kp (kp = d padded to 32)."""
+    k3 = 3 * ((d + 31) // 32 * 32)
+    r = roofline_flops("bf16", 2.0 * pairs * k3, avg_launch_ms)
+    r["flops_note"] = ("tensor-core work of the two-piece scan, 2 x pairs x 3 kp (hi.hi + lo.hi + hi.lo); "
+                       "the FP32 problem itself is 2 x pairs x d = %.4g flop per launch" % (2.0 * pairs * d))
+    return r
 
 
 def roofline_bytes(bytes_per_launch, avg_launch_ms, kernel="scan"):
@@ -397,16 +408,19 @@ def allknn_mode(cx, X, mode, overfetch, steps, warmup):
     ms, launches, main_ms, main_launches, clocks = timed_device_steps(cx, h, step, steps, warmup)
     ids_host = ids_d.cpu().numpy().view(np.uint32)
     dists_host = dists_d.cpu().numpy()
+    plain_tc = mode == "fp32" and cx.get(h, "last_plain_tc") == 1.0
+    fallbacks = cx.get(h, "fallbacks")
     cx.L.ssg_destroy(h)
     avg = main_ms / max(1, main_launches)
     q_per_launch = n * steps / max(1, main_launches)
-    roof = roofline_flops(mode, 2.0 * q_per_launch * n * d, avg)
-    if mode == "bf16" and n == 1_000_000 and d == 96 and main_launches == steps:
+    roof = (plain_tc_roofline(q_per_launch * n, d, avg) if plain_tc
+            else roofline_flops(mode, 2.0 * q_per_launch * n * d, avg))
+    if mode == "bf16" and n == 1_000_000 and d == 96 and main_launches == steps and overfetch == HEADLINE_TRAFFIC_OVERFETCH:
         roof["traffic"] = HEADLINE_SCAN_TRAFFIC
         roof["traffic_note"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch at over-fetch %.2f, "
                                 "one ncu capture (profiles/tc_wide_bf16_allknn.md)" % HEADLINE_TRAFFIC_OVERFETCH)
     return {"ms_per_step": ms, "qps": cx.world * n / (ms / 1e3), "launches": launches, "roofline": roof,
-            "clocks": clocks, "ids": ids_host, "dists": dists_host}
+            "clocks": clocks, "ids": ids_host, "dists": dists_host, "fallbacks": fallbacks, "plain_tc": plain_tc}
 
 
 def allknn_e2e(cx, X, mode, overfetch, steps):
@@ -500,6 +514,7 @@ def gpu_arm(args):
             plain = allknn_mode(cx, X, "fp32", None, args.steps, args.warmup)
             modes["fp32"] = {"value": plain["qps"], "ms_per_step": plain["ms_per_step"],
                              "roofline": plain["roofline"], "steps": args.steps, "warmup": args.warmup,
+                             "fallbacks": plain["fallbacks"], "plain_on_tensor_cores": plain["plain_tc"],
                              "note": "plain FP32 method: results identical to ExhaustiveSearch's (lanes=1 sums)"}
         else:
             # replicas: the plain method runs once, untimed, for the over-fetch calibration
@@ -599,9 +614,11 @@ def search_entry(cx, name, X, Q, k, mode, steps, warmup, desc, roof_fn, parity_l
     gi = ids_d.cpu().numpy().view(np.uint32).copy()
     gd = dists_d.cpu().numpy().copy()
     fallbacks = cx.get(h, "fallbacks")
+    plain_tc = mode == "fp32" and cx.get(h, "last_plain_tc") == 1.0
     L.ssg_destroy(h)
     del Qd, ids_d, dists_d
-    roof = roof_fn(main_ms / max(1, main_launches))
+    avg = main_ms / max(1, main_launches)
+    roof = plain_tc_roofline(m * n, d, avg) if plain_tc else roof_fn(avg)
     # end to end: create from pinned host memory + search from host + results to host
     Xp, Qp = cx.pinned(X), cx.pinned(Q)
     oi = torch.empty((m, k), dtype=torch.int32).pin_memory()
@@ -640,7 +657,7 @@ def search_entry(cx, name, X, Q, k, mode, steps, warmup, desc, roof_fn, parity_l
     return {"workload": desc, "metric": "queries/s", "value": m / (ms / 1e3), "unit": "queries/s",
             "ms_per_step": ms, "steps": steps, "warmup": warmup, "mode": mode,
             "dtype": "u64" if name == "hamming" else ("f32" if mode == "fp32" else mode),
-            "roofline": roof, "parity": parity, "fallbacks": fallbacks,
+            "roofline": roof, "parity": parity, "fallbacks": fallbacks, "plain_on_tensor_cores": plain_tc,
             "cpu_baseline": cpu,
             "e2e": {"value": m / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(X.nbytes + Q.nbytes),
                     "d2h_bytes_per_step": int(m * k * 8)},

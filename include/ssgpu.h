@@ -151,13 +151,19 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * (1 = time the scan kernel with events), "graphs" (0 = no CUDA-graph replay
  * in ssg_search_batches), "wide" (0 = BF16 scans in 128 x 128 tiles instead
  * of 128 x 256), "locality" (0 = BF16 allknn scans in id order instead of
- * the pivot-grouped order; results are identical either way).  Unknown keys
- * return SSG_EINVAL. */
+ * the pivot-grouped order; results are identical either way), "plain_tc"
+ * (0 = keep the plain method on the CUDA cores; by default SqL2, L2,
+ * NormCosine and InnerProduct with dim <= 128 and at least 4096 objects run
+ * it on the tensor cores: a two-piece BF16 scan whose candidates are
+ * re-scored in exact FP32 and certified complete, uncertified queries
+ * recomputed by the exact scan -- results identical either way).  Unknown
+ * keys return SSG_EINVAL. */
 int ssg_set_param(ssg_index *idx, const char *key, double value);
 /* Readable keys: the tunables plus "n", "dim", "metric", "precision",
  * "main_kernel_ms" / "main_kernel_launches" (accumulated while profiling),
  * "kernel_launches" (kernels launched by the last call), "fallbacks" (queries
- * the last plain call recomputed with the exact scan), "max_x_sq",
+ * the last plain call recomputed with the exact scan), "last_plain_tc"
+ * (1 when the last plain call ran on the tensor cores), "max_x_sq",
  * "device_bytes". */
 int ssg_get_param(ssg_index *idx, const char *key, double *value);
 

@@ -107,6 +107,14 @@ struct ssg_index {
     // rows) and of the current queries
     DevBuf gm_db, gm_q;
     int64_t gm_rows = -1;
+    // the plain method on the tensor cores: two-piece BF16 tiles of the
+    // database in the database role (ps_db, with |x|^2 per padded row in
+    // ps_norm) and, for allknn, in the query role (ps_dbq), built for
+    // ps_rows rows; the current queries' tiles (ps_q)
+    DevBuf ps_db, ps_dbq, ps_norm, ps_q;
+    int64_t ps_rows = -1, ps_qrows = -1;
+    int plain_tc_param = 1;
+    int last_plain_tc = 0;  // 1: the last plain-method search ran on the tensor cores
     int64_t smp_r = 0, smp_n = -1, smp_rows = 0;
     DevBuf red[2];  // segment-reduction passes (merge_groups) ping-pong
     // learned shortlist (trained model, whether searches use it, recall target)
@@ -686,13 +694,177 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
     return SSG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The plain FP32 method on the tensor cores.  Every element is split into two
+// BF16 pieces, x = hi + lo (+ a remainder below 2^-16 |x|); a tcgen05 scan
+// over K = 3 kp with database rows laid out [hi | lo | hi] and query rows
+// [hi | hi | lo] accumulates hi.hi + lo.hi + hi.lo in FP32, an approximation
+// of x.q within c |x| |q|, c = 3.05 2^-16 (the pieces left out) + 6.1 kp 2^-23
+// (FP32 accumulation of 3 kp products, counted at twice the truncating
+// adder's bound).  The scan keeps kk = k + margin approximate candidates per
+// query; the rerank computes their exact FP32 distances (the oracle's
+// sequential sums) and checks that the candidate gap covers twice the
+// approximation error plus the exact evaluation's own (a query whose margin is
+// not provably enough is recomputed by the exact direct scan), so the result
+// is the plain method's, bit for bit.
+// ---------------------------------------------------------------------------
+
+// Split K of the plain method on the tensor cores, 0 when it does not apply
+// (metric, dimension, or no scan kernel holds the tiles and the heaps).
+int plain_tc_k(const ssg_index *idx, int kk) {
+    const int metric = idx->metric;
+    if (metric != SSG_METRIC_SQL2 && metric != SSG_METRIC_L2 && metric != SSG_METRIC_NORMCOSINE &&
+        metric != SSG_METRIC_IP)
+        return 0;
+    const int k3 = 3 * ssg::tc_padded_k(idx->dim);
+    if (k3 > 384) return 0;
+    return (ssg::tc_wide_fits(k3, kk) || ssg::tc_pair_fits(k3, kk)) ? k3 : 0;
+}
+
+// Two-piece tiles of the database (database role; the query role as well for
+// allknn), |x|^2 per padded row, and max |x|^2 for the dot metrics' check
+// (the squared-distance metrics keep it current on every append).
+int ensure_plain_tiles(ssg_index *idx, bool query_role) {
+    const int64_t tiles = (ssg::tc_tiles(idx->n) + 1) / 2 * 2;
+    const size_t tb = ssg::tc_tile_bytes(3 * ssg::tc_padded_k(idx->dim));
+    const float *x = static_cast<const float *>(idx->db.p);
+    if (idx->ps_rows != idx->n) {
+        idx->ps_qrows = -1;
+        SSG_CK(idx->ps_db.ensure(size_t(tiles) * tb), "allocating split database tiles");
+        SSG_CK(ssg::launch_bf16_tiles(x, idx->n, idx->dim, tiles, static_cast<uint8_t *>(idx->ps_db.p), idx->stream,
+                                      &idx->last_launches, nullptr, 1),
+               "building split database tiles");
+        SSG_CK(idx->ps_norm.ensure(size_t(tiles) * 128 * 4), "allocating split tile norms");
+        SSG_CK(ssg::launch_tc_norms(SSG_METRIC_SQL2, x, idx->n, idx->dim, tiles * 128,
+                                    static_cast<float *>(idx->ps_norm.p), idx->stream, &idx->last_launches),
+               "computing split tile norms");
+        if (!is_sq_metric(idx->metric)) {
+            SSG_CK(idx->sq_norm.ensure(size_t(idx->n) * 4), "allocating squared norms");
+            SSG_CK(idx->sq_max.ensure(16), "allocating the norm maximum");
+            SSG_CK(cudaMemsetAsync(idx->sq_max.p, 0, 4, idx->stream), "clearing the norm maximum");
+            SSG_CK(ssg::launch_row_sq_norms(x, idx->n, idx->dim, static_cast<float *>(idx->sq_norm.p),
+                                            static_cast<float *>(idx->sq_max.p), idx->stream, &idx->last_launches),
+                   "computing squared norms");
+            SSG_CK(cudaMemcpyAsync(&idx->max_x_sq, idx->sq_max.p, 4, cudaMemcpyDeviceToHost, idx->stream),
+                   "reading the norm maximum");
+        }
+        SSG_CK(cudaStreamSynchronize(idx->stream), "building split database tiles");
+        idx->ps_rows = idx->n;
+    }
+    if (query_role && idx->ps_qrows != idx->n) {
+        SSG_CK(idx->ps_dbq.ensure(size_t(tiles) * tb), "allocating split query-role tiles");
+        SSG_CK(ssg::launch_bf16_tiles(x, idx->n, idx->dim, tiles, static_cast<uint8_t *>(idx->ps_dbq.p),
+                                      idx->stream, &idx->last_launches, nullptr, 2),
+               "building split query-role tiles");
+        idx->ps_qrows = idx->n;
+    }
+    return SSG_OK;
+}
+
+int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
+                 float *d_dists, bool queries_are_db, int kk, int k3) {
+    const bool sq = is_sq_metric(idx->metric);
+    const int kp = ssg::tc_padded_k(idx->dim);
+    SSG_RC(ensure_plain_tiles(idx, queries_are_db));
+    const int64_t qctas = (m + 127) / 128;
+    const int64_t n_tiles = ssg::tc_tiles(idx->n);
+    int64_t splits = idx->splits_param > 0 ? idx->splits_param : wave_splits(qctas, ssg::device_sm_count(), n_tiles);
+    splits = std::max<int64_t>(1, std::min<int64_t>(splits, n_tiles));
+    const int segs = int(splits) * ssg::tc_segments_per_split(1);
+    const size_t per_query = size_t(segs) * kk * 8;
+    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
+    chunk = std::min<int64_t>(chunk, qctas * 128);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    SSG_CK(idx->flags.ensure(size_t(m) * 4 + 16), "allocating query flags");
+    SSG_CK(cudaMemsetAsync(idx->flags.p, 0, size_t(m) * 4 + 16, idx->stream), "clearing query flags");
+    SSG_CK(idx->qsq.ensure(size_t(chunk) * 4 + 16), "allocating query norms");
+    const size_t tb = ssg::tc_tile_bytes(k3);
+    const uint8_t *qtiles = static_cast<const uint8_t *>(idx->ps_dbq.p);
+    if (!queries_are_db) {
+        const int64_t qt_alloc = (qctas + 1) / 2 * 2;  // even: the pair scan reads query tiles in pairs
+        SSG_CK(idx->ps_q.ensure(size_t(qt_alloc) * tb), "allocating split query tiles");
+        SSG_CK(ssg::launch_bf16_tiles(dq, m, idx->dim, qt_alloc, static_cast<uint8_t *>(idx->ps_q.p), idx->stream,
+                                      &idx->last_launches, nullptr, 2),
+               "building split query tiles");
+        qtiles = static_cast<const uint8_t *>(idx->ps_q.p);
+    }
+    uint32_t *qbound = nullptr;
+    if (splits > 1) {
+        SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
+        qbound = static_cast<uint32_t *>(idx->qbound.p);
+    }
+    // |a - a_exact| <= c |x| |q| (see above) plus the exact evaluation's own
+    // error: (d + 2) 2^-24 |x| |q| for a dot product; the squared-distance
+    // metrics add c |x| |q| <= c/2 (|x| + |q|)^2 to the GEMM-form allowance
+    // 4 (d + 2) 2^-24 (|x| + |q|)^2
+    const float c = 3.05f * 1.52587890625e-5f + 6.1f * float(kp) * 1.1920929e-7f;
+    const float ulp24 = 5.9604645e-8f;
+    int *flags = static_cast<int *>(idx->flags.p);
+    int *flag_count = flags + m;
+    float *qsq = static_cast<float *>(idx->qsq.p);
+    ScanTimer timer(idx);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        if (qbound) SSG_CK(cudaMemsetAsync(qbound, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
+        SSG_RC(timer.begin());
+        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->ps_db.p),
+                                   static_cast<const float *>(idx->ps_norm.p), idx->n, mc, k3, kk, int(splits),
+                                   static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
+                                   idx->stream, &idx->last_launches, nullptr, nullptr, nullptr, true, idx->wave_param,
+                                   idx->pair_param != 0, qbound),
+               "launching the split tensor-core scan");
+        SSG_RC(timer.end());
+        const float *qc = dq + size_t(c0) * idx->dim;
+        SSG_CK(ssg::launch_row_sq_norms(qc, mc, idx->dim, qsq, qsq + chunk, idx->stream, &idx->last_launches),
+               "computing query norms");
+        ssg::FinalizeArgs f{};
+        SSG_RC(reduce_segments(idx, static_cast<const uint64_t *>(idx->cand.p), mc, segs, kk, &f.cand, &f.segs));
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        f.n_rows = idx->n;
+        f.check = sq ? 1 : 2;
+        f.q_sq = qsq;
+        f.max_x_sq = idx->max_x_sq;
+        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c : c + float(idx->dim + 2) * ulp24;
+        f.n_total = idx->n;
+        f.flags = flags + c0;
+        f.flag_count = flag_count;
+        SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc, nullptr,
+                                           idx->stream, &idx->last_launches),
+               "launching the rerank kernel");
+        SSG_RC(timer.collect());
+    }
+    int status = 0, nflag = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaMemcpyAsync(&nflag, flag_count, sizeof(int), cudaMemcpyDeviceToHost, idx->stream), "reading flags");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the split tensor-core scan");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the split tensor-core scan gave up (code %d)", status);
+    idx->last_fallbacks = nflag;
+    return run_fallback(idx, dq, m, k, exclude_self, flags, nflag, d_ids, d_dists);
+}
+
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db);
 int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                    uint32_t *d_ids, float *d_dists, bool queries_are_db);
 
-// Dispatch: BF16 tensor-core mode, Hamming, or the plain FP32 method (GEMM
-// form when its heaps fit, otherwise the exact direct scan).
+// Databases below this many rows keep the plain method on the CUDA cores
+// (the split tiles would cost more than the scan they speed up).
+constexpr int64_t kPlainTcMinRows = 4096;
+
+// Dispatch: BF16 tensor-core mode, Hamming, or the plain FP32 method (on the
+// tensor cores in split form where it applies, else GEMM form when its heaps
+// fit, otherwise the exact direct scan).
 int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
             uint32_t *d_ids, float *d_dists, bool queries_are_db = false) {
     if (idx->prec != SSG_PREC_FP32 && !idx->plain_param) {
@@ -700,6 +872,17 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
         return run_knn_tc(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db);
     }
     idx->last_fallbacks = 0;
+    idx->last_plain_tc = 0;
+    if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param && idx->plain_tc_param &&
+        idx->n >= kPlainTcMinRows && !idx->capturing) {
+        const int take = k + (exclude_self ? 1 : 0);
+        const int kk = int(std::min<int64_t>(int64_t(take) + gemm_margin(idx, take), idx->n));
+        const int k3 = plain_tc_k(idx, kk);
+        idx->last_plain_tc = k3 > 0;
+        if (k3 > 0)
+            return run_plain_tc(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
+                                queries_are_db, kk, k3);
+    }
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
         const int take = k + (exclude_self ? 1 : 0);
         int64_t kk = is_sq_metric(idx->metric) ? int64_t(take) + gemm_margin(idx, take) : take;
@@ -1675,6 +1858,8 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->exact_scan_param = value != 0.0;
     } else if (k == "plain") {
         idx->plain_param = value != 0.0;
+    } else if (k == "plain_tc") {
+        idx->plain_tc_param = value != 0.0;
     } else if (k == "learned") {
         idx->learned_param = value != 0.0;
     } else if (k == "learned_target") {
@@ -1734,6 +1919,8 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "margin") *value = idx->margin_param;
     else if (k == "exact_scan") *value = idx->exact_scan_param;
     else if (k == "plain") *value = idx->plain_param;
+    else if (k == "plain_tc") *value = idx->plain_tc_param;
+    else if (k == "last_plain_tc") *value = idx->last_plain_tc;
     else if (k == "learned") *value = idx->learned_param;
     else if (k == "learned_target") *value = idx->learned_target;
     else if (k == "train_hard") *value = idx->train_hard;
@@ -1963,7 +2150,8 @@ void ssg_destroy(ssg_index *idx) {
         b->release();
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand, &idx->fb_qn, &idx->tc_smp, &idx->tc_smp_norm, &idx->f_out, &idx->f_cnt,
-                      &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out, &idx->gm_db, &idx->gm_q})
+                      &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out, &idx->gm_db, &idx->gm_q,
+                      &idx->ps_db, &idx->ps_dbq, &idx->ps_norm, &idx->ps_q, &idx->qbound})
         b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);

@@ -59,12 +59,14 @@ struct FinalizeArgs {
     float *out_dists;
     // optional: per-query object ids for exclude_self (overrides self_base)
     const int64_t *self_ids = nullptr;
-    // optional completeness check of a GEMM-form candidate list (SqL2 / L2):
-    // flags[j] = 1 (and *flag_count += 1) when the kk approximate candidates
-    // do not provably contain the exact top (k + exclude_self).
+    // optional completeness check of an approximate candidate list: flags[j]
+    // = 1 (and *flag_count += 1) when the kk approximate candidates do not
+    // provably contain the exact top (k + exclude_self).  1: GEMM-form keys
+    // of SqL2 / L2 (|x|^2 - 2 x.q), error err_scale (|x|max + |q|)^2; 2:
+    // dot-product keys (-x.q), error err_scale |x|max |q|.
     int check = 0;
     const float *q_sq = nullptr;   // |q|^2 per query
-    float max_x_sq = 0.0f;         // max |x|^2 over the database
+    float max_x_sq = 0.0f;         // max |x|^2 over the database (the metric's rows as stored)
     float err_scale = 0.0f;        // c * d * 2^-24 (see finalize_rerank_kernel)
     int64_t n_total = 0;           // database rows
     int *flags = nullptr;
@@ -113,9 +115,11 @@ bool tc_pair_fits(int kp, int kk);
 // Sorted candidate segments the scan writes per (query, split) for a CTA with
 // `qt` query tiles (the epilogue splits a tile's columns between warps).
 int tc_segments_per_split(int qt);
-// With a map, tile row i holds source row map[i].
+// With a map, tile row i holds source row map[i].  split: 0 = BF16 rows
+// (K = kp); 1 = database rows of the two-piece plain method, [hi | lo | hi];
+// 2 = its query rows, [hi | hi | lo] (K = 3 kp; see bf16_tile_kernel).
 cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
-                              cudaStream_t st, int *launches, const uint32_t *map = nullptr);
+                              cudaStream_t st, int *launches, const uint32_t *map = nullptr, int split = 0);
 // |x|^2 (SqL2/L2) or 1/|x| (Cosine) per padded row (of source row map[i]
 // with a map).
 cudaError_t launch_tc_norms(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded, float *out,

@@ -106,7 +106,24 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         }
         s2[i] = key;
     }
-    if (f.check && threadIdx.x == 0) {
+    if (f.check == 2 && threadIdx.x == 0) {
+        // Completeness for dot-product keys (a = -x.q approximated): with
+        // |a - (D - c)| <= E = err_scale |x|max |q| + 2^-22 (c the metric's
+        // constant, 1 for NormCosine), the same argument as below.
+        const int take = f.k_out + (f.exclude_self ? 1 : 0);
+        int nv = 0;
+        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
+        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
+            const float E = f.err_scale * sqrtf(f.max_x_sq) * sqrtf(f.q_sq[j]) + 2.4e-7f;
+            const float a_take = key_dist(s1[take - 1]);
+            const float a_last = key_dist(s1[f.kk - 1]);
+            if (!(a_last > a_take + 2.0f * E)) {
+                f.flags[j] = 1;
+                atomicAdd(f.flag_count, 1);
+            }
+        }
+    }
+    if (f.check == 1 && threadIdx.x == 0) {
         // Completeness of a GEMM-form candidate list.  With a = |x|^2 - 2 x.q
         // the approximate value and D the exact difference-form distance,
         // |a + |q|^2 - D| <= E = err_scale * (sqrt(max|x|^2) + |q|)^2.  Every

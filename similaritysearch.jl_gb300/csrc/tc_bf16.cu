@@ -90,26 +90,34 @@ int metric_class(int metric) {
 // Prep: FP32 rows -> BF16 tiles in the swizzled operand layout.
 // ---------------------------------------------------------------------------
 // Tile row i holds source row map[i] when a map is given (a reordering of the
-// database), row i otherwise.
-__global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kp, int64_t tiles,
+// database), row i otherwise.  split != 0: the two-piece form of the plain
+// method on the tensor cores -- each element x as hi = bf16(x) and
+// lo = bf16(x - hi), laid out along K in three segments of kp: database rows
+// (split 1) as [hi | lo | hi], query rows (split 2) as [hi | hi | lo], so one
+// product over K = 3 kp accumulates hi.hi + lo.hi + hi.lo.
+__global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kp, int split, int64_t tiles,
                                  const uint32_t *__restrict__ map, uint8_t *__restrict__ out) {
-    const int chunks_per_row = kp / 8;
+    const int kout = split ? 3 * kp : kp;
+    const int chunks_per_row = kout / 8;
     const int64_t total = tiles * TILE * chunks_per_row;
-    const size_t tile_bytes = size_t(TILE) * kp * 2;
+    const size_t tile_bytes = size_t(TILE) * kout * 2;
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
          i += int64_t(gridDim.x) * blockDim.x) {
         const int cidx = int(i % chunks_per_row);
         const int64_t grow = i / chunks_per_row;
         const int64_t tile = grow / TILE;
         const int r = int(grow % TILE);
-        const int col0 = cidx * 8;
+        const int col0 = cidx * 8;             // column of the tile (kp is a multiple of 8)
+        const int seg = col0 / kp, scol = col0 % kp;
+        const bool low = (split == 1 && seg == 1) || (split == 2 && seg == 2);
         __align__(16) __nv_bfloat16 v[8];
         const int64_t src = grow < rows && map ? int64_t(map[grow]) : grow;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             float f = 0.0f;
-            if (grow < rows && col0 + e < dim) f = x[src * dim + col0 + e];
-            v[e] = __float2bfloat16_rn(f);
+            if (grow < rows && scol + e < dim) f = x[src * dim + scol + e];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+            v[e] = low ? __float2bfloat16_rn(f - __bfloat162float(hi)) : hi;
         }
         const int blk = col0 / KBE;
         const uint32_t off = tc::swizzled_offset(uint32_t(r), uint32_t((col0 % KBE) * 2), SW);
@@ -1178,14 +1186,14 @@ bool tc_choose(int kp, int kk, int *qt, int *stages) {
 }
 
 cudaError_t launch_bf16_tiles(const float *x, int64_t rows, int64_t dim, int64_t tiles, uint8_t *out,
-                              cudaStream_t st, int *launches, const uint32_t *map) {
+                              cudaStream_t st, int *launches, const uint32_t *map, int split) {
     const int kp = tc_padded_k(dim);
-    const int64_t total = tiles * TILE * (kp / 8);
+    const int64_t total = tiles * TILE * ((split ? 3 : 1) * kp / 8);
     int64_t blocks = (total + 255) / 256;
     if (blocks > 148 * 64) blocks = 148 * 64;
     if (blocks < 1) blocks = 1;
     if (launches) *launches += 1;
-    bf16_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kp, tiles, map, out);
+    bf16_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kp, split, tiles, map, out);
     return cudaGetLastError();
 }
 
@@ -1273,8 +1281,11 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     a.rot = rot;
     a.qbound = qbound;
     int qt = 1, stages = 0, kst = 0, pkst = 0;
-    const bool use_pair = wide && pair && pair_choose(a.kp, kk, &pkst);
-    const bool use_wide = !use_pair && wide && wide_choose(a.kp, kk, &kst);
+    // CTA pairs when asked for, or when the one-CTA wide scan does not fit
+    // (their ring stages are half the size)
+    const bool wide_ok = wide && wide_choose(a.kp, kk, &kst);
+    const bool use_pair = wide && (pair || !wide_ok) && pair_choose(a.kp, kk, &pkst);
+    const bool use_wide = !use_pair && wide_ok;
     if (!use_pair && !use_wide && !tc_choose(a.kp, kk, &qt, &stages)) return cudaErrorInvalidValue;
     if ((perm || rot) && qt != 1) return cudaErrorInvalidValue;
     if (qt_out) *qt_out = qt;

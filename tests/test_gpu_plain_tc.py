@@ -1,0 +1,116 @@
+"""The plain FP32 method on the tensor cores (two-piece BF16 scan, exact FP32
+rerank of k + margin candidates, completeness check, exact-scan fallback)
+against the oracle's sequential (lanes=1) ExhaustiveSearch restatement
+(src/exact/sequential-exhaustive.jl:60-78, src/allknn.jl:66-110): ids and
+distances bit-identical, for every metric it serves, across dimensions,
+k, allknn, and inputs made to defeat the check (exact ties, duplicates),
+where the fallback must take over.  The same searches with "plain_tc" off
+(CUDA-core GEMM form) give the same arrays."""
+import numpy as np
+import pytest
+
+from conftest import load_package
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+METRICS = {"sql2": "SqL2", "l2": "L2", "normcosine": "NormCosine", "ip": "InnerProduct"}
+
+
+@pytest.fixture(scope="module")
+def ss():
+    mod = load_package()
+    mod.build()
+    return mod
+
+
+def make(name, n, m, d, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, d), dtype=np.float32)
+    Q = rng.standard_normal((m, d), dtype=np.float32)
+    if name == "normcosine":
+        X /= np.linalg.norm(X, axis=1, keepdims=True)
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    return X, Q
+
+
+def run(ss, name, X, Q, k, plain_tc=1):
+    idx = ss.GPUExhaustiveSearch(getattr(ss.Dist, METRICS[name])(), ss.MatrixDatabase.from_rows(X))
+    idx.set_param("plain_tc", plain_tc)
+    ids, dists = ss.searchbatch(idx, ss.GenericContext(logger=None), ss.MatrixDatabase.from_rows(Q), k)
+    return ids.T, dists.T, idx
+
+
+@pytest.mark.parametrize("name", list(METRICS))
+@pytest.mark.parametrize("d,k", [(8, 1), (33, 10), (96, 32), (128, 10), (100, 64)])
+def test_plain_tc_searchbatch_bitexact(ss, name, d, k):
+    X, Q = make(name, 20000, 300, d, seed=d * 7 + k)
+    gi, gd, idx = run(ss, name, X, Q, k)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.searchbatch(name, X, Q, k, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri)
+    assert np.array_equal(gd, rd)
+    # the margin is rarely too small on Gaussian data
+    assert idx.get_param("fallbacks") <= 0.05 * Q.shape[0]
+    ci, cd, cidx = run(ss, name, X, Q, k, plain_tc=0)
+    assert cidx.get_param("last_plain_tc") == 0.0
+    assert np.array_equal(gi, ci) and np.array_equal(gd, cd)
+
+
+@pytest.mark.parametrize("name", ["sql2", "normcosine"])
+def test_plain_tc_allknn_bitexact(ss, name):
+    rng = np.random.default_rng(61)
+    C = rng.standard_normal((40, 96), dtype=np.float32)
+    X = C[rng.integers(0, 40, 12000)] + 0.3 * rng.standard_normal((12000, 96), dtype=np.float32)
+    if name == "normcosine":
+        X /= np.linalg.norm(X, axis=1, keepdims=True)
+    idx = ss.GPUExhaustiveSearch(getattr(ss.Dist, METRICS[name])(), ss.MatrixDatabase.from_rows(X))
+    ids, dists = ss.allknn(idx, ss.GenericContext(logger=None), 32, exclude_self=True)
+    assert idx.get_param("last_plain_tc") == 1.0
+    rows = np.sort(rng.choice(12000, size=300, replace=False))
+    ri, rd = O.allknn_rows(name, X, 33, rows, lanes=1, nthreads=O.num_threads())
+    for r, j in enumerate(rows):
+        keep = [t for t in range(33) if ri[r, t] != j + 1][:32]
+        assert np.array_equal(ids.T[j], ri[r, keep])
+        assert np.array_equal(dists.T[j], rd[r, keep])
+
+
+@pytest.mark.parametrize("name", list(METRICS))
+def test_plain_tc_ties_defeat_the_check_and_fall_back(ss, name):
+    """Each database row repeated 40 times: every candidate list is a run of
+    equal distances, no margin certifies it, and the fallback's exact scan
+    answers; ids still follow the (distance, id) order."""
+    rng = np.random.default_rng(62)
+    base = rng.standard_normal((200, 48), dtype=np.float32)
+    if name == "normcosine":
+        base /= np.linalg.norm(base, axis=1, keepdims=True)
+    X = np.repeat(base, 40, axis=0)
+    Q = base[:50] + np.float32(1e-3) * rng.standard_normal((50, 48), dtype=np.float32)
+    if name == "normcosine":
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    gi, gd, idx = run(ss, name, X, Q, 10)
+    assert idx.get_param("last_plain_tc") == 1.0
+    assert idx.get_param("fallbacks") == 50
+    ri, rd = O.searchbatch(name, X, Q, 10, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
+def test_plain_tc_wide_magnitudes_and_appends(ss):
+    """Log-normal row norms over several binades, then appended rows: the
+    split tiles are rebuilt for the grown database."""
+    rng = np.random.default_rng(63)
+    X = rng.standard_normal((9000, 64), dtype=np.float32) * rng.lognormal(0, 2.0, (9000, 1)).astype(np.float32)
+    Q = rng.standard_normal((200, 64), dtype=np.float32) * rng.lognormal(0, 2.0, (200, 1)).astype(np.float32)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X))
+    ctx = ss.GenericContext(logger=None)
+    ids, dists = ss.searchbatch(idx, ctx, ss.MatrixDatabase.from_rows(Q), 10)
+    ri, rd = O.searchbatch("sql2", X, Q, 10, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(ids.T, ri) and np.array_equal(dists.T, rd)
+    extra = Q[:30] + np.float32(1e-2)
+    for row in extra:
+        ss.push_item_b(idx, ctx, row)
+    X2 = np.concatenate([X, extra])
+    ids, dists = ss.searchbatch(idx, ctx, ss.MatrixDatabase.from_rows(Q), 10)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.searchbatch("sql2", X2, Q, 10, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(ids.T, ri) and np.array_equal(dists.T, rd)
