@@ -772,7 +772,7 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
     splits = std::max<int64_t>(1, std::min<int64_t>(splits, n_tiles));
     const int segs = int(splits) * ssg::tc_segments_per_split(1);
     const size_t per_query = size_t(segs) * kk * 8;
-    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
+    int64_t chunk = std::max<int64_t>(256, int64_t((size_t(1) << 30) / per_query) / 256 * 256);
     chunk = std::min<int64_t>(chunk, qctas * 128);
     SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
     SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
@@ -1003,7 +1003,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     // chunk the queries (a multiple of the CTA's query rows) to bound scratch
     const int segs = int(splits) * ssg::tc_segments_per_split(qt);
     const size_t per_query = size_t(segs) * kk * 8;
-    int64_t chunk = std::max<int64_t>(qrows, int64_t((size_t(1) << 30) / per_query) / qrows * qrows);
+    int64_t chunk = std::max<int64_t>(2 * qrows, int64_t((size_t(1) << 30) / per_query) / (2 * qrows) * (2 * qrows));
     chunk = std::min<int64_t>(chunk, (m + qrows - 1) / qrows * qrows);
     SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
     SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
@@ -1137,7 +1137,7 @@ int run_knn_tc_filter(ssg_index *idx, const void *dq, const float *dqn, int64_t 
     }
     const int segs_s = ssg::tc_segments_per_split(1);
     const size_t per_query = size_t(fcap) * 8 + size_t(std::max(kk, segs_s * kSampleK)) * 8 + 8;
-    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(512) << 20) / per_query) / 128 * 128);
+    int64_t chunk = std::max<int64_t>(256, int64_t((size_t(512) << 20) / per_query) / 256 * 256);
     chunk = std::min<int64_t>(chunk, (m + 127) / 128 * 128);
     SSG_CK(idx->f_out.ensure(size_t(chunk) * fcap * 8), "allocating filter lists");
     SSG_CK(idx->f_cnt.ensure(size_t(chunk) * 4), "allocating filter counts");
