@@ -531,11 +531,14 @@ def gpu_arm(args):
         if cx.rank == 0:
             print(json.dumps({"metric": METRIC, "value": head["qps"], "unit": "queries/s", "n": n, "mode": mode,
                               "overfetch": of, "ms_per_step": head["ms_per_step"], "roofline": head["roofline"],
+                              "fallbacks": head["fallbacks"], "plain_on_tensor_cores": head["plain_tc"],
                               "gpu_launches": head["launches"]}), flush=True)
         return
     e2e = allknn_e2e(cx, X, mode, of, max(1, min(args.steps, 3)))
     modes[mode] = {"value": head["qps"], "ms_per_step": head["ms_per_step"],
-                   "roofline_frac": head["roofline"]["frac"], "overfetch": of}
+                   "roofline_frac": head["roofline"]["frac"], "overfetch": of if mode != "fp32" else None}
+    if mode == "fp32":
+        modes[mode].update({"fallbacks": head["fallbacks"], "plain_on_tensor_cores": head["plain_tc"]})
     four_k = None
     if mode == "bf16" and cx.world == 1 and not args.no_plain:
         # the configuration as written: FP32 rerank of the top 4k candidates

@@ -697,16 +697,20 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
 // ---------------------------------------------------------------------------
 // The plain FP32 method on the tensor cores.  Every element is split into two
 // BF16 pieces, x = hi + lo (+ a remainder below 2^-16 |x|); a tcgen05 scan
-// over K = 3 kp with database rows laid out [hi | lo | hi] and query rows
-// [hi | hi | lo] accumulates hi.hi + lo.hi + hi.lo in FP32, an approximation
-// of x.q within c |x| |q|, c = 3.05 2^-16 (the pieces left out) + 6.1 kp 2^-23
-// (FP32 accumulation of 3 kp products, counted at twice the truncating
-// adder's bound).  The scan keeps kk = k + margin approximate candidates per
-// query; the rerank computes their exact FP32 distances (the oracle's
-// sequential sums) and checks that the candidate gap covers twice the
-// approximation error plus the exact evaluation's own (a query whose margin is
-// not provably enough is recomputed by the exact direct scan), so the result
-// is the plain method's, bit for bit.
+// over K = 3 kp with database rows laid out [lo | hi | hi] and query rows
+// [hi | lo | hi] accumulates lo.hi + hi.lo + hi.hi in FP32, an approximation
+// of x.q within c |x| |q|:
+//   3.05 2^-16   the terms left out (lo.lo and both remainders);
+//   2.2 kp 2^-23 FP32 accumulation: the 2 kp small products come first, so
+//                their partial sums stay below 2^-7 |x||q|; the kp products
+//                hi.hi then add at most 2^-23 of the largest magnitude in
+//                the adder per product (17 terms per 16-product MMA), about
+//                1.1 kp 2^-23 |x||q| in all, counted twice.
+// The scan keeps kk = k + margin approximate candidates per query; the rerank
+// computes their exact FP32 distances (the oracle's sequential sums) and
+// certifies that no object outside the list can reach the result (rerank.cu,
+// the completeness check); a query it cannot certify is recomputed by the
+// exact direct scan, so the result is the plain method's, bit for bit.
 // ---------------------------------------------------------------------------
 
 // Split K of the plain method on the tensor cores, 0 when it does not apply
@@ -799,7 +803,7 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
     // error: (d + 2) 2^-24 |x| |q| for a dot product; the squared-distance
     // metrics add c |x| |q| <= c/2 (|x| + |q|)^2 to the GEMM-form allowance
     // 4 (d + 2) 2^-24 (|x| + |q|)^2
-    const float c = 3.05f * 1.52587890625e-5f + 6.1f * float(kp) * 1.1920929e-7f;
+    const float c = 3.05f * 1.52587890625e-5f + 2.2f * float(kp) * 1.1920929e-7f;
     const float ulp24 = 5.9604645e-8f;
     int *flags = static_cast<int *>(idx->flags.p);
     int *flag_count = flags + m;

@@ -67,7 +67,7 @@ struct FinalizeArgs {
     int check = 0;
     const float *q_sq = nullptr;   // |q|^2 per query
     float max_x_sq = 0.0f;         // max |x|^2 over the database (the metric's rows as stored)
-    float err_scale = 0.0f;        // c * d * 2^-24 (see finalize_rerank_kernel)
+    float err_scale = 0.0f;        // the error bound's scale (see the check's kinds above)
     int64_t n_total = 0;           // database rows
     int *flags = nullptr;
     int *flag_count = nullptr;

@@ -106,48 +106,44 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         }
         s2[i] = key;
     }
-    if (f.check == 2 && threadIdx.x == 0) {
-        // Completeness for dot-product keys (a = -x.q approximated): with
-        // |a - (D - c)| <= E = err_scale |x|max |q| + 2^-22 (c the metric's
-        // constant, 1 for NormCosine), the same argument as below.
-        const int take = f.k_out + (f.exclude_self ? 1 : 0);
-        int nv = 0;
-        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
-        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
-            const float E = f.err_scale * sqrtf(f.max_x_sq) * sqrtf(f.q_sq[j]) + 2.4e-7f;
-            const float a_take = key_dist(s1[take - 1]);
-            const float a_last = key_dist(s1[f.kk - 1]);
-            if (!(a_last > a_take + 2.0f * E)) {
-                f.flags[j] = 1;
-                atomicAdd(f.flag_count, 1);
-            }
-        }
-    }
-    if (f.check == 1 && threadIdx.x == 0) {
-        // Completeness of a GEMM-form candidate list.  With a = |x|^2 - 2 x.q
-        // the approximate value and D the exact difference-form distance,
-        // |a + |q|^2 - D| <= E = err_scale * (sqrt(max|x|^2) + |q|)^2.  Every
-        // item of the exact top `take` then has a <= a_take + 2E, so if the
-        // last kept candidate has a_last > a_take + 2E (+ the sqrt-collision
-        // allowance of L2), nothing outside the list can belong to it.
-        const int take = f.k_out + (f.exclude_self ? 1 : 0);
-        int nv = 0;
-        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
-        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
-            const float qs = f.q_sq[j];
-            const float r = sqrtf(f.max_x_sq) + sqrtf(qs);
-            const float E = f.err_scale * r * r;
-            const float a_take = key_dist(s1[take - 1]);
-            const float a_last = key_dist(s1[f.kk - 1]);
-            float slack = 2.0f * E;
-            if (METRIC == L2) slack += 8.0f * 5.96e-8f * fabsf(a_take + qs + E);
-            if (!(a_last > a_take + slack)) {
-                f.flags[j] = 1;
-                atomicAdd(f.flag_count, 1);
-            }
-        }
-    }
     block_bitonic_sort(s2, P2);
+    if (f.check && threadIdx.x == 0) {
+        // Completeness of an approximate candidate list.  An object y left
+        // out has an approximate key a(y) >= a_last (the list's last), and
+        // its exact FP32 distance D(y) >= a(y) + c - E, where c turns keys
+        // into distances and E bounds the approximation and evaluation errors:
+        //   check 1 (keys |x|^2 - 2 x.q of SqL2 / L2): c = |q|^2,
+        //           E = err_scale (sqrt(max |x|^2) + |q|)^2;
+        //   check 2 (keys -x.q): c = 1 for NormCosine, 0 for InnerProduct,
+        //           E = err_scale sqrt(max |x|^2) |q| + 2^-22.
+        // If a_last + c - E exceeds the exact distance of the take-th
+        // re-ranked candidate (for L2 its square, widened by 2^-20 so that
+        // sqrt rounding cannot tie), y ranks behind it: the list holds the
+        // exact top `take`.  Evaluated in double.
+        const int take = f.k_out + (f.exclude_self ? 1 : 0);
+        int nv = 0;
+        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
+        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
+            const double qs = double(f.q_sq[j]);
+            const double xm = sqrt(double(f.max_x_sq));
+            double c, E;
+            if (f.check == 1) {
+                const double r = xm + sqrt(qs);
+                c = qs;
+                E = double(f.err_scale) * r * r;
+            } else {
+                c = METRIC == NORMCOSINE ? 1.0 : 0.0;
+                E = double(f.err_scale) * xm * sqrt(qs) + 2.384185791015625e-7;
+            }
+            const double lower = double(key_dist(s1[f.kk - 1])) + c - E;
+            double dtake = double(key_dist(s2[take - 1]));
+            if (METRIC == L2) dtake = dtake * dtake * (1.0 + 9.5367431640625e-7);
+            if (!(lower > dtake)) {
+                f.flags[j] = 1;
+                atomicAdd(f.flag_count, 1);
+            }
+        }
+    }
     if (threadIdx.x == 0) {
         uint32_t *oi = f.out_ids + size_t(j) * f.k_out;
         float *od = f.out_dists + size_t(j) * f.k_out;

@@ -93,8 +93,9 @@ int metric_class(int metric) {
 // database), row i otherwise.  split != 0: the two-piece form of the plain
 // method on the tensor cores -- each element x as hi = bf16(x) and
 // lo = bf16(x - hi), laid out along K in three segments of kp: database rows
-// (split 1) as [hi | lo | hi], query rows (split 2) as [hi | hi | lo], so one
-// product over K = 3 kp accumulates hi.hi + lo.hi + hi.lo.
+// (split 1) as [lo | hi | hi], query rows (split 2) as [hi | lo | hi], so one
+// product over K = 3 kp accumulates lo.hi + hi.lo + hi.hi, the two small
+// terms first (while the accumulator, and so its rounding, is small).
 __global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kp, int split, int64_t tiles,
                                  const uint32_t *__restrict__ map, uint8_t *__restrict__ out) {
     const int kout = split ? 3 * kp : kp;
@@ -109,7 +110,7 @@ __global__ void bf16_tile_kernel(const float *__restrict__ x, int64_t rows, int 
         const int r = int(grow % TILE);
         const int col0 = cidx * 8;             // column of the tile (kp is a multiple of 8)
         const int seg = col0 / kp, scol = col0 % kp;
-        const bool low = (split == 1 && seg == 1) || (split == 2 && seg == 2);
+        const bool low = (split == 1 && seg == 0) || (split == 2 && seg == 1);
         __align__(16) __nv_bfloat16 v[8];
         const int64_t src = grow < rows && map ? int64_t(map[grow]) : grow;
 #pragma unroll

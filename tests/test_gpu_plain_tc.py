@@ -42,11 +42,13 @@ def run(ss, name, X, Q, k, plain_tc=1):
 
 
 @pytest.mark.parametrize("name", list(METRICS))
-@pytest.mark.parametrize("d,k", [(8, 1), (33, 10), (96, 32), (128, 10), (100, 64)])
-def test_plain_tc_searchbatch_bitexact(ss, name, d, k):
+@pytest.mark.parametrize("d,k,on_tc", [(8, 1, 1), (33, 10, 1), (96, 32, 1), (128, 10, 1), (24, 48, 1), (100, 64, 0)])
+def test_plain_tc_searchbatch_bitexact(ss, name, d, k, on_tc):
+    # (100, 64): 80 candidates per query do not fit the scans' on-chip heaps
+    # next to K = 384 tiles, so the plain method stays on the CUDA cores
     X, Q = make(name, 20000, 300, d, seed=d * 7 + k)
     gi, gd, idx = run(ss, name, X, Q, k)
-    assert idx.get_param("last_plain_tc") == 1.0
+    assert idx.get_param("last_plain_tc") == on_tc
     ri, rd = O.searchbatch(name, X, Q, k, lanes=1, nthreads=O.num_threads())
     assert np.array_equal(gi, ri)
     assert np.array_equal(gd, rd)
