@@ -718,16 +718,31 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
 // exact direct scan, so the result is the plain method's, bit for bit.
 // ---------------------------------------------------------------------------
 
-// Split K of the plain method on the tensor cores, 0 when it does not apply
-// (metric, dimension, or no scan kernel holds the tiles and the heaps).
-int plain_tc_k(const ssg_index *idx, int kk) {
+// How the plain method runs on the tensor cores: split K (0: it does not
+// apply -- metric, dimension, or no scan kernel holds the tiles and the
+// heaps), candidates kept per heap and candidates re-ranked per query.  The
+// list is k + margin long (margin 0.45 k, at least 8: fallbacks cost far more
+// than a longer list).  Each heap keeps the whole list when the one-CTA wide
+// scan holds it with four ring stages or more; otherwise each of a query
+// tile's two column heaps keeps half of it (the completeness check accounts
+// for what a half-heap dropped), and the CTA-pair scan is the last resort.
+struct PlainTcPlan {
+    int k3 = 0, h = 0, rr = 0;
+};
+PlainTcPlan plain_tc_plan(const ssg_index *idx, int take) {
     const int metric = idx->metric;
     if (metric != SSG_METRIC_SQL2 && metric != SSG_METRIC_L2 && metric != SSG_METRIC_NORMCOSINE &&
         metric != SSG_METRIC_IP)
-        return 0;
+        return {};
     const int k3 = 3 * ssg::tc_padded_k(idx->dim);
-    if (k3 > 384) return 0;
-    return (ssg::tc_wide_fits(k3, kk) || ssg::tc_pair_fits(k3, kk)) ? k3 : 0;
+    if (k3 > 384) return {};
+    const int margin = idx->margin_param > 0 ? idx->margin_param : std::max(8, (9 * take + 19) / 20);
+    const int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
+    if (ssg::tc_wide_stages(k3, kk) >= 4) return {k3, kk, kk};
+    const int h = (kk + 1) / 2;
+    if (ssg::tc_wide_stages(k3, h) >= 3) return {k3, h, 2 * h};
+    if (ssg::tc_pair_fits(k3, kk)) return {k3, kk, kk};
+    return {};
 }
 
 // Two-piece tiles of the database (database role; the query role as well for
@@ -771,7 +786,8 @@ int ensure_plain_tiles(ssg_index *idx, bool query_role) {
 }
 
 int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
-                 float *d_dists, bool queries_are_db, int kk, int k3) {
+                 float *d_dists, bool queries_are_db, const PlainTcPlan &plan) {
+    const int kk = plan.h, k3 = plan.k3;
     const bool sq = is_sq_metric(idx->metric);
     const int kp = ssg::tc_padded_k(idx->dim);
     SSG_RC(ensure_plain_tiles(idx, queries_are_db));
@@ -838,6 +854,7 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
         f.n_rows = idx->n;
+        f.rerank = std::min(plan.rr, f.segs * kk);
         f.check = sq ? 1 : 2;
         f.q_sq = qsq;
         f.max_x_sq = idx->max_x_sq;
@@ -884,13 +901,11 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
     idx->last_plain_tc = 0;
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param && idx->plain_tc_param &&
         idx->n >= kPlainTcMinRows && !idx->capturing) {
-        const int take = k + (exclude_self ? 1 : 0);
-        const int kk = int(std::min<int64_t>(int64_t(take) + gemm_margin(idx, take), idx->n));
-        const int k3 = plain_tc_k(idx, kk);
-        idx->last_plain_tc = k3 > 0;
-        if (k3 > 0)
+        const PlainTcPlan plan = plain_tc_plan(idx, k + (exclude_self ? 1 : 0));
+        idx->last_plain_tc = plan.k3 > 0;
+        if (plan.k3 > 0)
             return run_plain_tc(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
-                                queries_are_db, kk, k3);
+                                queries_are_db, plan);
     }
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
         const int take = k + (exclude_self ? 1 : 0);

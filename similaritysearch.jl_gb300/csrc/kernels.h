@@ -74,6 +74,10 @@ struct FinalizeArgs {
     // rows of the database the keys index: a key with a larger id is treated
     // as empty instead of being read (the rerank kernels set it always)
     int64_t n_rows = 0;
+    // candidates re-ranked per query, from the merged segments (0: kk, the
+    // segment length).  More than kk when each heap kept only part of the
+    // list (the plain method's half heaps on the tensor cores).
+    int rerank = 0;
 };
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t st, int *launches);
 
@@ -111,6 +115,8 @@ bool tc_choose(int kp, int kk, int *qt, int *stages);
 // Whether the wide scan's heaps and ring fit for this K and candidate count
 // (one CTA, or a CTA pair with half-size ring stages).
 bool tc_wide_fits(int kp, int kk);
+// Ring stages of the wide scan at this K and candidate count (0: it does not fit).
+int tc_wide_stages(int kp, int kk);
 bool tc_pair_fits(int kp, int kk);
 // Sorted candidate segments the scan writes per (query, split) for a CTA with
 // `qt` query tiles (the epilogue splits a tile's columns between warps).

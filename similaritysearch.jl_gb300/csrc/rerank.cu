@@ -94,9 +94,10 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
     for (int i = threadIdx.x; i < P1; i += blockDim.x) s1[i] = i < total ? src[i] : KEY_EMPTY;
     if (f.segs > 1) block_bitonic_sort(s1, P1);
     else __syncthreads();
+    const int rr = f.rerank ? f.rerank : f.kk;
     for (int i = threadIdx.x; i < P2; i += blockDim.x) {
         uint64_t key = KEY_EMPTY;
-        if (i < f.kk) {
+        if (i < rr) {
             const uint64_t ak = s1[i];
             if (ak != KEY_EMPTY && int64_t(key_id0(ak)) < f.n_rows) {
                 const uint32_t id0 = key_id0(ak);
@@ -109,21 +110,29 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
     block_bitonic_sort(s2, P2);
     if (f.check && threadIdx.x == 0) {
         // Completeness of an approximate candidate list.  An object y left
-        // out has an approximate key a(y) >= a_last (the list's last), and
-        // its exact FP32 distance D(y) >= a(y) + c - E, where c turns keys
-        // into distances and E bounds the approximation and evaluation errors:
+        // out was either dropped by a full heap (or a merge of segments), so
+        // its approximate key a(y) is at least that segment's last key, or
+        // sits in a segment behind the re-ranked list: a(y) >= a_low =
+        // min(last key of every full segment, last re-ranked key).  Its exact
+        // FP32 distance D(y) >= a(y) + c - E, where c turns keys into
+        // distances and E bounds the approximation and evaluation errors:
         //   check 1 (keys |x|^2 - 2 x.q of SqL2 / L2): c = |q|^2,
         //           E = err_scale (sqrt(max |x|^2) + |q|)^2;
         //   check 2 (keys -x.q): c = 1 for NormCosine, 0 for InnerProduct,
         //           E = err_scale sqrt(max |x|^2) |q| + 2^-22.
-        // If a_last + c - E exceeds the exact distance of the take-th
+        // If a_low + c - E exceeds the exact distance of the take-th
         // re-ranked candidate (for L2 its square, widened by 2^-20 so that
         // sqrt rounding cannot tie), y ranks behind it: the list holds the
         // exact top `take`.  Evaluated in double.
         const int take = f.k_out + (f.exclude_self ? 1 : 0);
         int nv = 0;
-        while (nv < f.kk && s1[nv] != KEY_EMPTY) ++nv;
-        if (nv == f.kk && int64_t(f.kk) < f.n_total && take <= f.kk) {
+        while (nv < rr && s1[nv] != KEY_EMPTY) ++nv;
+        if (nv == rr && int64_t(rr) < f.n_total && take <= rr) {
+            uint64_t low = s1[rr - 1];
+            for (int sgi = 0; sgi < f.segs; ++sgi) {
+                const uint64_t last = src[size_t(sgi) * f.kk + f.kk - 1];
+                if (last != KEY_EMPTY && last < low) low = last;
+            }
             const double qs = double(f.q_sq[j]);
             const double xm = sqrt(double(f.max_x_sq));
             double c, E;
@@ -135,7 +144,7 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
                 c = METRIC == NORMCOSINE ? 1.0 : 0.0;
                 E = double(f.err_scale) * xm * sqrt(qs) + 2.384185791015625e-7;
             }
-            const double lower = double(key_dist(s1[f.kk - 1])) + c - E;
+            const double lower = double(key_dist(low)) + c - E;
             double dtake = double(key_dist(s2[take - 1]));
             if (METRIC == L2) dtake = dtake * dtake * (1.0 + 9.5367431640625e-7);
             if (!(lower > dtake)) {
@@ -168,7 +177,9 @@ cudaError_t launch_finalize_rerank(int metric, const FinalizeArgs &f, const floa
                                    int64_t dim, const float *q, const float *q_norm, cudaStream_t st,
                                    int *launches) {
     const int P1 = next_pow2(int64_t(f.segs) * f.kk);
-    const int P2 = next_pow2(f.kk);
+    const int rr = f.rerank ? f.rerank : f.kk;
+    if (rr > f.segs * f.kk) return cudaErrorInvalidValue;
+    const int P2 = next_pow2(rr);
     const size_t smem = size_t(P1 + P2) * 8;
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
     if (launches) *launches += 1;

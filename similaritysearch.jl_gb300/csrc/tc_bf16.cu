@@ -1155,6 +1155,10 @@ bool tc_wide_fits(int kp, int kk) {
     int kst = 0;
     return wide_choose(kp, kk, &kst);
 }
+int tc_wide_stages(int kp, int kk) {
+    int kst = 0;
+    return wide_choose(kp, kk, &kst) ? kst : 0;
+}
 bool pair_choose(int kp, int kk, int *kst);
 bool tc_pair_fits(int kp, int kk) {
     int kst = 0;
