@@ -13,8 +13,11 @@ overfetch x (k+1) candidates per object, re-ranked in exact FP32.  The
 over-fetch is the smallest of a fixed ladder whose recall@32 against the
 plain method reaches 0.99 on calibration rows; recall is then reported on
 other rows against the oracle and the FP64 ranking.  `modes.fp32` is the
-plain FP32 method (results identical to ExhaustiveSearch's), timed with the
-same steps.
+plain FP32 method (results identical to ExhaustiveSearch's) as the library
+runs it by default, on the tensor cores in two-piece BF16 form with the
+exact rerank and completeness check, timed with the same steps;
+`modes.fp32_cuda_cores` is the same method on the CUDA cores (FP32 FMA
+GEMM form, its roofline against the FP32 peak), timed with fewer steps.
 
 `suite` carries the other configurations in the same run, each with its own
 roofline, CPU baseline, end-to-end figure and clocks: C1 (searchbatch SqL2,
@@ -393,10 +396,10 @@ def allknn_once(cx, h, n):
     return ids_d.cpu().numpy().view(np.uint32), dists_d.cpu().numpy()
 
 
-def allknn_mode(cx, X, mode, overfetch, steps, warmup):
+def allknn_mode(cx, X, mode, overfetch, steps, warmup, **params):
     torch = cx.torch
     n, d = X.shape
-    h = cx.create(cx.N.METRIC_NORMCOSINE, cx.N.ELEM_F32, X, PREC[mode])
+    h = cx.create(cx.N.METRIC_NORMCOSINE, cx.N.ELEM_F32, X, PREC[mode], **params)
     if mode != "fp32" and overfetch is not None:
         cx.set(h, "overfetch", overfetch)
     ids_d = torch.empty((n, K), dtype=torch.int32, device="cuda")
@@ -515,7 +518,17 @@ def gpu_arm(args):
             modes["fp32"] = {"value": plain["qps"], "ms_per_step": plain["ms_per_step"],
                              "roofline": plain["roofline"], "steps": args.steps, "warmup": args.warmup,
                              "fallbacks": plain["fallbacks"], "plain_on_tensor_cores": plain["plain_tc"],
-                             "note": "plain FP32 method: results identical to ExhaustiveSearch's (lanes=1 sums)"}
+                             "note": "plain FP32 method: results identical to ExhaustiveSearch's (lanes=1 sums); "
+                                     "two-piece BF16 tensor-core scan, exact FP32 rerank, certified complete"}
+            cc_steps = max(1, min(args.steps, 2))
+            cc = allknn_mode(cx, X, "fp32", None, cc_steps, 1, plain_tc=0)
+            modes["fp32_cuda_cores"] = {
+                "value": cc["qps"], "ms_per_step": cc["ms_per_step"], "roofline": cc["roofline"],
+                "steps": cc_steps, "warmup": 1, "fallbacks": cc["fallbacks"],
+                "ids_equal_to_fp32": bool(np.array_equal(cc["ids"], plain["ids"])),
+                "dists_equal_to_fp32": bool(np.array_equal(cc["dists"], plain["dists"])),
+                "note": "the plain method on the CUDA cores (FP32 FMA GEMM form + exact rerank)"}
+            del cc
         else:
             # replicas: the plain method runs once, untimed, for the over-fetch calibration
             plain = allknn_mode(cx, X, "fp32", None, 1, 0)
@@ -565,6 +578,9 @@ def gpu_arm(args):
         modes["fp32"]["recall@10"] = recall_rows(gold, plain["ids"][rows], 10)
         modes["fp32"]["recall@32"] = recall_rows(gold, plain["ids"][rows], K)
         modes["speedup_vs_fp32"] = head["qps"] / plain["qps"]
+        if "fp32_cuda_cores" in modes:
+            modes["speedup_vs_fp32_cuda_cores"] = head["qps"] / modes["fp32_cuda_cores"]["value"]
+            modes["fp32_tc_speedup_vs_cuda_cores"] = plain["qps"] / modes["fp32_cuda_cores"]["value"]
     line = {
         "metric": METRIC, "value": head["qps"], "unit": "queries/s", "n_gpus": cx.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -676,10 +692,15 @@ def suite_c1(cx, args):
     desc = "searchbatch SqL2, n=100,000, d=128, m=1,000, k=10 (N(0,1) data)"
     e = search_entry(cx, "sql2", X, Q, k, "fp32", max(args.steps, 20), args.warmup, desc,
                      lambda ms: roofline_flops("fp32", 2.0 * m * n * d, ms))
+    cc = search_entry(cx, "sql2", X, Q, k, "fp32", max(args.steps, 20), args.warmup, desc,
+                      lambda ms: roofline_flops("fp32", 2.0 * m * n * d, ms), cpu_budget=1.0, plain_tc=0)
     bf = search_entry(cx, "sql2", X, Q, k, "bf16", max(args.steps, 20), args.warmup, desc,
                       lambda ms: roofline_flops("bf16", 2.0 * m * n * d, ms), cpu_budget=1.0, overfetch=2.0)
     e["modes"] = {"bf16": {"value": bf["value"], "ms_per_step": bf["ms_per_step"], "overfetch": 2.0,
-                           "recall@k_vs_oracle": bf["parity"]["recall@k"], "roofline": bf["roofline"]}}
+                           "recall@k_vs_oracle": bf["parity"]["recall@k"], "roofline": bf["roofline"]},
+                  "fp32_cuda_cores": {"value": cc["value"], "ms_per_step": cc["ms_per_step"],
+                                      "roofline": cc["roofline"], "parity": cc["parity"], "e2e": cc["e2e"],
+                                      "note": "the plain method on the CUDA cores (FP32 FMA GEMM form)"}}
     return e
 
 
