@@ -721,11 +721,15 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
 // How the plain method runs on the tensor cores: split K (0: it does not
 // apply -- metric, dimension, or no scan kernel holds the tiles and the
 // heaps), candidates kept per heap and candidates re-ranked per query.  The
-// list is k + margin long (margin 0.45 k, at least 8: fallbacks cost far more
-// than a longer list).  Each heap keeps the whole list when the one-CTA wide
-// scan holds it with four ring stages or more; otherwise each of a query
-// tile's two column heaps keeps half of it (the completeness check accounts
-// for what a half-heap dropped), and the CTA-pair scan is the last resort.
+// list is k + margin long (margin 0.45 k, at least 8: a fallback costs far
+// more than a longer list).  Each heap keeps the whole list when the one-CTA
+// wide scan holds it with four ring stages or more.  Otherwise each of a
+// query tile's two column heaps keeps part of it, as many as fit beside four
+// ring stages and at least half the list: the completeness check then stops
+// at the first full heap's last key, so the pair of heaps holds more than
+// the list itself (about 2 x 32 for 33 neighbours on 96 dimensions, where
+// 2 x 24 left 3.5 % of the queries uncertified).  The CTA-pair scan is the
+// last resort.
 struct PlainTcPlan {
     int k3 = 0, h = 0, rr = 0;
 };
@@ -739,7 +743,11 @@ PlainTcPlan plain_tc_plan(const ssg_index *idx, int take) {
     const int margin = idx->margin_param > 0 ? idx->margin_param : std::max(8, (9 * take + 19) / 20);
     const int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
     if (ssg::tc_wide_stages(k3, kk) >= 4) return {k3, kk, kk};
-    const int h = (kk + 1) / 2;
+    int h = (kk + 1) / 2;
+    if (ssg::tc_wide_stages(k3, h) >= 4) {
+        while (h < kk && ssg::tc_wide_stages(k3, h + 1) >= 4) ++h;
+        return {k3, h, 2 * h};
+    }
     if (ssg::tc_wide_stages(k3, h) >= 3) return {k3, h, 2 * h};
     if (ssg::tc_pair_fits(k3, kk)) return {k3, kk, kk};
     return {};
