@@ -182,7 +182,7 @@ def plain_tc_roofline(pairs, d, avg_launch_ms):
     BF16 products run over K = 3 kp (kp = d padded to 32)."""
     k3 = 3 * ((d + 31) // 32 * 32)
     r = roofline_flops("bf16", 2.0 * pairs * k3, avg_launch_ms)
-    r["flops_note"] = ("tensor-core work of the two-piece scan, 2 x pairs x 3 kp (hi.hi + lo.hi + hi.lo); "
+    r["flops_note"] = ("tensor-core work of the two-piece scan, 2 x pairs x 3 kp (lo.hi + hi.lo + hi.hi); "
                        "the FP32 problem itself is 2 x pairs x d = %.4g flop per launch" % (2.0 * pairs * d))
     return r
 
