@@ -87,7 +87,11 @@ struct ssg_index {
     // each query tile's scan, BF16 tiles and norms in that order; built for
     // loc_n rows (-1: none)
     DevBuf loc_perm, loc_rot, loc_tiles, loc_norm;
-    int64_t loc_n = -1;
+    int64_t loc_n = -1, loc_bf16_n = -1;
+    // the plain method's split tiles (both roles) and |x|^2 in that order,
+    // built for loc_ps_n rows (-1: none)
+    DevBuf loc_ps_db, loc_ps_dbq, loc_ps_norm;
+    int64_t loc_ps_n = -1;
     int locality_param = 1;
     int wide_param = 1;    // BF16 scan: 256-row database tiles per MMA
     int64_t wave_param = 0;  // wide scan: query tiles per launch (0: one launch)
@@ -250,6 +254,8 @@ int ensure_db_capacity(ssg_index *idx, int64_t rows) {
 // past the end when the database doubles as the query set (allknn).
 int build_tc_tiles(ssg_index *idx) {
     idx->loc_n = -1;
+    idx->loc_bf16_n = -1;
+    idx->loc_ps_n = -1;
     const int64_t tiles = (ssg::tc_tiles(idx->n) + 1) / 2 * 2;
     const size_t tb = ssg::tc_tile_bytes(idx->dim);
     SSG_CK(idx->tc_db.ensure(size_t(tiles) * tb), "allocating BF16 database tiles");
@@ -793,6 +799,12 @@ int ensure_plain_tiles(ssg_index *idx, bool query_role) {
     return SSG_OK;
 }
 
+// allknn's locality order needs at least this many rows (below it the order's
+// set-up would cost more than the heap insertions it saves)
+constexpr int64_t kLocalityMinRows = 32768;
+
+int ensure_plain_locality(ssg_index *idx);
+
 int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
                  float *d_dists, bool queries_are_db, const PlainTcPlan &plan) {
     const int kk = plan.h, k3 = plan.k3;
@@ -823,6 +835,22 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
                "building split query tiles");
         qtiles = static_cast<const uint8_t *>(idx->ps_q.p);
     }
+    // allknn in one launch: the database in its locality order (rows grouped
+    // by nearest pivot, each query tile starting at its own group), so the
+    // heaps hold near neighbours from the first tiles on and few later
+    // columns pass their bound
+    const uint8_t *dtiles = static_cast<const uint8_t *>(idx->ps_db.p);
+    const float *dnorm = static_cast<const float *>(idx->ps_norm.p);
+    const uint32_t *perm = nullptr;
+    const int *rot = nullptr;
+    if (queries_are_db && idx->locality_param && m == idx->n && idx->n >= kLocalityMinRows && chunk >= m) {
+        SSG_RC(ensure_plain_locality(idx));
+        qtiles = static_cast<const uint8_t *>(idx->loc_ps_dbq.p);
+        dtiles = static_cast<const uint8_t *>(idx->loc_ps_db.p);
+        dnorm = static_cast<const float *>(idx->loc_ps_norm.p);
+        perm = static_cast<const uint32_t *>(idx->loc_perm.p);
+        rot = static_cast<const int *>(idx->loc_rot.p);
+    }
     uint32_t *qbound = nullptr;
     if (splits > 1) {
         SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
@@ -842,11 +870,10 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
         if (qbound) SSG_CK(cudaMemsetAsync(qbound, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
         SSG_RC(timer.begin());
-        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->ps_db.p),
-                                   static_cast<const float *>(idx->ps_norm.p), idx->n, mc, k3, kk, int(splits),
-                                   static_cast<uint64_t *>(idx->cand.p), static_cast<int *>(idx->status.p),
-                                   idx->stream, &idx->last_launches, nullptr, nullptr, nullptr, true, idx->wave_param,
-                                   idx->pair_param != 0, qbound),
+        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, k3, kk,
+                                   int(splits), static_cast<uint64_t *>(idx->cand.p),
+                                   static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr, perm,
+                                   rot, true, idx->wave_param, idx->pair_param != 0, qbound),
                "launching the split tensor-core scan");
         SSG_RC(timer.end());
         const float *qc = dq + size_t(c0) * idx->dim;
@@ -939,22 +966,22 @@ int64_t overfetch_kk(const ssg_index *idx, int take) {
     return std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
 }
 
-// allknn's locality order needs at least this many rows (below it the order's
-// set-up would cost more than the heap insertions it saves)
-constexpr int64_t kLocalityMinRows = 32768;
-
 // Builds allknn's locality order (tc_bf16.cu, launch_locality_order): P
 // evenly spaced rows as pivots (about 1024 rows per pivot), each row's
-// nearest pivot by a kk = 1 scan of the BF16 tiles against the pivots' tiles,
-// rows grouped by pivot, and the BF16 tiles and norms rebuilt in that order.
-// Kept until the database changes.
-int ensure_locality(ssg_index *idx) {
+// nearest pivot by a kk = 1 scan of the database's tiles in the query role
+// (`qtiles`: the BF16 tiles, or the plain method's split tiles with `split`
+// 2) against the pivots' tiles, rows grouped by pivot; position -> id in
+// loc_perm and each query tile's start tile in loc_rot.  The order only
+// groups rows: any assignment to pivots gives the same results.  Kept until
+// the database changes.
+int ensure_locality_order(ssg_index *idx, const uint8_t *qtiles, int split) {
     if (idx->loc_n == idx->n) return SSG_OK;
     const int64_t n = idx->n;
     const int P = int(std::min<int64_t>(16384, std::max<int64_t>(128, (n / 1024 + 127) / 128 * 128)));
     std::vector<uint32_t> prow(static_cast<size_t>(P));
     for (int i = 0; i < P; ++i) prow[size_t(i)] = uint32_t(int64_t(i) * n / P);
-    const size_t tb = ssg::tc_tile_bytes(idx->dim);
+    const int64_t kdim = split ? 3 * ssg::tc_padded_k(idx->dim) : idx->dim;
+    const size_t tb = ssg::tc_tile_bytes(kdim);
     const int64_t ptiles = (ssg::tc_tiles(P) + 1) / 2 * 2;
     const int segs = ssg::tc_segments_per_split(1);
     DevBuf prow_d, pt, pn, work;
@@ -966,7 +993,7 @@ int ensure_locality(ssg_index *idx) {
     const float *x = static_cast<const float *>(idx->db.p);
     const uint32_t *pmap = static_cast<const uint32_t *>(prow_d.p);
     SSG_CK(ssg::launch_bf16_tiles(x, P, idx->dim, ptiles, static_cast<uint8_t *>(pt.p), idx->stream,
-                                  &idx->last_launches, pmap),
+                                  &idx->last_launches, pmap, split ? 1 : 0),
            "building pivot tiles");
     SSG_CK(ssg::launch_tc_norms(idx->metric, x, P, idx->dim, ptiles * 128, static_cast<float *>(pn.p), idx->stream,
                                 &idx->last_launches, pmap),
@@ -980,27 +1007,19 @@ int ensure_locality(ssg_index *idx) {
     int *count = reinterpret_cast<int *>(pivot + n);
     SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
     SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
-    SSG_CK(ssg::launch_tc_scan(idx->metric, static_cast<const uint8_t *>(idx->tc_db.p),
-                               static_cast<const uint8_t *>(pt.p), static_cast<const float *>(pn.p), P, n, idx->dim,
-                               1, 1, cand, static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches,
-                               nullptr),
+    // the split tiles' K only fits the wide scan
+    SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles, static_cast<const uint8_t *>(pt.p),
+                               static_cast<const float *>(pn.p), P, n, kdim, 1, 1, cand,
+                               static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr, nullptr,
+                               nullptr, split != 0),
            "launching the pivot scan");
-    const int64_t qtiles = ssg::tc_tiles(n);
+    const int64_t qtiles_n = ssg::tc_tiles(n);
     SSG_CK(idx->loc_perm.ensure(size_t(n) * 4), "allocating the locality order");
-    SSG_CK(idx->loc_rot.ensure(size_t(qtiles) * 4), "allocating scan start tiles");
-    uint32_t *perm = static_cast<uint32_t *>(idx->loc_perm.p);
-    SSG_CK(ssg::launch_locality_order(cand, n, segs, P, pivot, count, count + P, count + 2 * P, perm,
-                                      static_cast<int *>(idx->loc_rot.p), idx->stream, &idx->last_launches),
+    SSG_CK(idx->loc_rot.ensure(size_t(qtiles_n) * 4), "allocating scan start tiles");
+    SSG_CK(ssg::launch_locality_order(cand, n, segs, P, pivot, count, count + P, count + 2 * P,
+                                      static_cast<uint32_t *>(idx->loc_perm.p), static_cast<int *>(idx->loc_rot.p),
+                                      idx->stream, &idx->last_launches),
            "ordering rows by pivot");
-    const int64_t tiles = (qtiles + 1) / 2 * 2;
-    SSG_CK(idx->loc_tiles.ensure(size_t(tiles) * tb), "allocating locality-ordered tiles");
-    SSG_CK(ssg::launch_bf16_tiles(x, n, idx->dim, tiles, static_cast<uint8_t *>(idx->loc_tiles.p), idx->stream,
-                                  &idx->last_launches, perm),
-           "building locality-ordered tiles");
-    SSG_CK(idx->loc_norm.ensure(size_t(tiles) * 128 * 4), "allocating locality-ordered norms");
-    SSG_CK(ssg::launch_tc_norms(idx->metric, x, n, idx->dim, tiles * 128, static_cast<float *>(idx->loc_norm.p),
-                                idx->stream, &idx->last_launches, perm),
-           "computing locality-ordered norms");
     int status = 0;
     SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
            "reading the status word");
@@ -1008,6 +1027,55 @@ int ensure_locality(ssg_index *idx) {
     if (status != 0)
         return fail(idx, SSG_ETIMEOUT, "a bounded wait in the pivot scan gave up (code %d)", status);
     idx->loc_n = n;
+    return SSG_OK;
+}
+
+// The BF16 tiles and norms in the locality order (built from the BF16 tiles'
+// pivot scan when no order exists yet).
+int ensure_locality(ssg_index *idx) {
+    if (idx->loc_n == idx->n && idx->loc_tiles.p && idx->loc_norm.p && idx->loc_bf16_n == idx->n) return SSG_OK;
+    SSG_RC(ensure_locality_order(idx, static_cast<const uint8_t *>(idx->tc_db.p), 0));
+    const int64_t n = idx->n;
+    const float *x = static_cast<const float *>(idx->db.p);
+    const uint32_t *perm = static_cast<const uint32_t *>(idx->loc_perm.p);
+    const int64_t tiles = (ssg::tc_tiles(n) + 1) / 2 * 2;
+    SSG_CK(idx->loc_tiles.ensure(size_t(tiles) * ssg::tc_tile_bytes(idx->dim)), "allocating locality-ordered tiles");
+    SSG_CK(ssg::launch_bf16_tiles(x, n, idx->dim, tiles, static_cast<uint8_t *>(idx->loc_tiles.p), idx->stream,
+                                  &idx->last_launches, perm),
+           "building locality-ordered tiles");
+    SSG_CK(idx->loc_norm.ensure(size_t(tiles) * 128 * 4), "allocating locality-ordered norms");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, x, n, idx->dim, tiles * 128, static_cast<float *>(idx->loc_norm.p),
+                                idx->stream, &idx->last_launches, perm),
+           "computing locality-ordered norms");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building locality-ordered tiles");
+    idx->loc_bf16_n = n;
+    return SSG_OK;
+}
+
+// The plain method's split tiles (database and query roles) and |x|^2 in the
+// locality order, from a pivot scan of the split tiles.
+int ensure_plain_locality(ssg_index *idx) {
+    if (idx->loc_ps_n == idx->n && idx->loc_n == idx->n) return SSG_OK;
+    SSG_RC(ensure_locality_order(idx, static_cast<const uint8_t *>(idx->ps_dbq.p), 2));
+    const int64_t n = idx->n;
+    const float *x = static_cast<const float *>(idx->db.p);
+    const uint32_t *perm = static_cast<const uint32_t *>(idx->loc_perm.p);
+    const int64_t tiles = (ssg::tc_tiles(n) + 1) / 2 * 2;
+    const size_t tb = ssg::tc_tile_bytes(3 * ssg::tc_padded_k(idx->dim));
+    SSG_CK(idx->loc_ps_db.ensure(size_t(tiles) * tb), "allocating locality-ordered split tiles");
+    SSG_CK(ssg::launch_bf16_tiles(x, n, idx->dim, tiles, static_cast<uint8_t *>(idx->loc_ps_db.p), idx->stream,
+                                  &idx->last_launches, perm, 1),
+           "building locality-ordered split tiles");
+    SSG_CK(idx->loc_ps_dbq.ensure(size_t(tiles) * tb), "allocating locality-ordered split query tiles");
+    SSG_CK(ssg::launch_bf16_tiles(x, n, idx->dim, tiles, static_cast<uint8_t *>(idx->loc_ps_dbq.p), idx->stream,
+                                  &idx->last_launches, perm, 2),
+           "building locality-ordered split query tiles");
+    SSG_CK(idx->loc_ps_norm.ensure(size_t(tiles) * 128 * 4), "allocating locality-ordered norms");
+    SSG_CK(ssg::launch_tc_norms(SSG_METRIC_SQL2, x, n, idx->dim, tiles * 128,
+                                static_cast<float *>(idx->loc_ps_norm.p), idx->stream, &idx->last_launches, perm),
+           "computing locality-ordered norms");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "building locality-ordered split tiles");
+    idx->loc_ps_n = n;
     return SSG_OK;
 }
 
@@ -2174,7 +2242,9 @@ void ssg_destroy(ssg_index *idx) {
     idx->tc_norm.release();
     idx->tc_q.release();
     idx->status.release();
-    for (DevBuf *b : {&idx->loc_perm, &idx->loc_rot, &idx->loc_tiles, &idx->loc_norm}) b->release();
+    for (DevBuf *b : {&idx->loc_perm, &idx->loc_rot, &idx->loc_tiles, &idx->loc_norm, &idx->loc_ps_db,
+                      &idx->loc_ps_dbq, &idx->loc_ps_norm})
+        b->release();
     ssg::learned_free(idx->learned);
     idx->learned = nullptr;
     for (DevBuf *b : {&idx->st_db, &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale,

@@ -116,3 +116,26 @@ def test_plain_tc_wide_magnitudes_and_appends(ss):
     assert idx.get_param("last_plain_tc") == 1.0
     ri, rd = O.searchbatch("sql2", X2, Q, 10, lanes=1, nthreads=O.num_threads())
     assert np.array_equal(ids.T, ri) and np.array_equal(dists.T, rd)
+
+
+@pytest.mark.parametrize("name", ["sql2", "ip"])
+def test_plain_tc_allknn_locality_order(ss, name):
+    """allknn over 40,000 rows scans the database in its locality order
+    (rows grouped by nearest pivot); the arrays equal the id-order scan's and
+    the oracle's rows."""
+    rng = np.random.default_rng(64)
+    C = rng.standard_normal((300, 64), dtype=np.float32)
+    X = C[rng.integers(0, 300, 40000)] + 0.4 * rng.standard_normal((40000, 64), dtype=np.float32)
+    idx = ss.GPUExhaustiveSearch(getattr(ss.Dist, METRICS[name])(), ss.MatrixDatabase.from_rows(X))
+    ctx = ss.GenericContext(logger=None)
+    ids, dists = ss.allknn(idx, ctx, 16, exclude_self=True)
+    assert idx.get_param("last_plain_tc") == 1.0
+    idx.set_param("locality", 0)
+    ids0, dists0 = ss.allknn(idx, ctx, 16, exclude_self=True)
+    assert np.array_equal(ids, ids0) and np.array_equal(dists, dists0)
+    rows = np.sort(rng.choice(40000, size=200, replace=False))
+    ri, rd = O.allknn_rows(name, X, 17, rows, lanes=1, nthreads=O.num_threads())
+    for r, j in enumerate(rows):
+        keep = [t for t in range(17) if ri[r, t] != j + 1][:16]
+        assert np.array_equal(ids.T[j], ri[r, keep])
+        assert np.array_equal(dists.T[j], rd[r, keep])
