@@ -42,6 +42,7 @@
 #include "kernels.h"
 #include "tc_ptx.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -740,6 +741,36 @@ cudaError_t launch_wide_mc(const TcArgs &a, int mc, cudaStream_t st, int64_t wav
     return launch_wide_t<KST, MC_DOT>(a, st, wave, launches);
 }
 
+// The database tiles seen by the tensor-map TMA as a 2D array of 64-byte
+// lines (32 BF16, already swizzled): line (tile * kblocks + kb) * 128 + r is
+// row r of K-block kb of a tile, so one 32 x 128 box is one tile's K-block,
+// copied verbatim (no swizzle mode: the bytes already are in the MMA's
+// layout).  The tile set holds an even number of tiles.
+cudaError_t database_line_map(const TcArgs &a, CUtensorMap *map) {
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+        encode = reinterpret_cast<EncodeFn>(fn);
+    }
+    if (reinterpret_cast<uintptr_t>(a.dt) % 16 != 0) return cudaErrorInvalidValue;
+    const cuuint64_t lines = cuuint64_t((a.n_tiles + 1) / 2 * 2) * cuuint64_t(a.kp / KBE) * TILE;
+    const cuuint64_t dims[2] = {cuuint64_t(KBE), lines};
+    const cuuint64_t strides[1] = {cuuint64_t(SW)};
+    const cuuint32_t box[2] = {cuuint32_t(KBE), cuuint32_t(TILE)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<uint8_t *>(a.dt), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // ---------------------------------------------------------------------------
 // The pair scan: the wide scan on CTA pairs (clusters of two) with M = 256
 // MMAs (tcgen05 cta_group::2).  Each CTA owns one 128-row query tile, as in
@@ -773,7 +804,8 @@ struct PairSmem {
 };
 
 template <int KST, int MC>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) tc_pair_kernel(TcArgs a) {
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1)
+    tc_pair_kernel(TcArgs a, const __grid_constant__ CUtensorMap dmap) {
     constexpr int CS = 2;
     constexpr int NACC = 2;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -787,9 +819,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
     uint64_t *bars = buf_base + size_t(TILE) * CS * kBufCap;
     uint64_t *a_full = bars;                 // this CTA's query tile landed
     uint64_t *pa_full = a_full + 1;          // (even CTA) the odd CTA's query tile landed
-    uint64_t *full = pa_full + 1;            // this CTA's half of stage s landed
-    uint64_t *pfull = full + KST;            // (even CTA) the odd CTA's half of stage s landed
-    uint64_t *empty = pfull + KST;           // the MMAs of stage s are done
+    uint64_t *full = pa_full + 1;            // (even CTA) both halves of stage s landed
+    uint64_t *empty = full + KST;            // the MMAs of stage s are done
     uint64_t *acc_full = empty + KST;        // accumulator b holds a finished wide tile
     uint64_t *acc_empty = acc_full + NACC;   // (even CTA) its epilogue warps released b
     uint64_t *pacc_empty = acc_empty + NACC; // (even CTA) the odd CTA's epilogue warps released b
@@ -815,7 +846,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
         tc::mbar_init(pa_full, 1);
         for (int s = 0; s < KST; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&pfull[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < NACC; ++b) {
@@ -849,36 +879,41 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
 
     if (warp == 0) {
         if (lane == 0) {
-            // producer: this CTA's query tile, then its half of every K-block
+            // producer: this CTA's query tile, then its half of every K-block.
+            // Both halves of stage s complete on the even CTA's full[s]: the
+            // even CTA arms it for both, the odd CTA's TMA counts its bytes
+            // there directly (cta_group::2), so no thread relays them.
             tc::mbar_arrive_expect_tx(a_full, uint32_t(tile_bytes));
             tc::bulk_g2s(sA, a.qt + size_t(qx) * tile_bytes, uint32_t(tile_bytes), a_full);
+            const uint32_t full0 = tc::mapa_shared(tc::smem_u32(full), 0);
             int issued = 0;
             for (int st = 0; st < steps; ++st) {
                 const int s = st % KST;
                 if (!tc::mbar_wait(&empty[s], ((st / KST) & 1) ^ 1, a.err, 1)) break;
                 const int u = st / kblocks, kb = st % kblocks;
-                const uint8_t *src = a.dt + size_t(2 * phys_wide(u) + rank) * tile_bytes + size_t(kb) * KBLK;
-                tc::mbar_arrive_expect_tx(&full[s], uint32_t(PKBLK));
-                tc::bulk_g2s(sB + size_t(s) * PKBLK, src, uint32_t(PKBLK), &full[s]);
+                const int64_t tile = 2 * phys_wide(u) + rank;
+                if (rank == 0) {
+                    tc::mbar_arrive_expect_tx(&full[s], uint32_t(2 * PKBLK));
+                    tc::bulk_g2s(sB + size_t(s) * PKBLK, a.dt + size_t(tile) * tile_bytes + size_t(kb) * KBLK,
+                                 uint32_t(PKBLK), &full[s]);
+                } else {
+                    tc::tma_load_2d_pair(sB + size_t(s) * PKBLK, &dmap, 0, int((tile * kblocks + kb) * TILE),
+                                         full0 + uint32_t(s * 8));
+                }
                 issued = st + 1;
             }
-            // wait (bounded) until every copy this thread issued has landed
+            // wait (bounded) until every copy of this CTA pair has landed
+            // (the even CTA's barriers count both halves; the final cluster
+            // barrier keeps the odd CTA alive until then)
             tc::mbar_wait(a_full, 0, a.err, 2);
-            for (int st = issued - KST < 0 ? 0 : issued - KST; st < issued; ++st)
-                tc::mbar_wait(&full[st % KST], (st / KST) & 1, a.err, 2);
+            if (rank == 0)
+                for (int st = issued - KST < 0 ? 0 : issued - KST; st < issued; ++st)
+                    tc::mbar_wait(&full[st % KST], (st / KST) & 1, a.err, 2);
         }
     } else if (warp == 1) {
         if (lane == 0 && rank == 1) {
-            // the odd CTA forwards its landed copies to the even CTA
-            const uint32_t r_pa = tc::mapa_shared(tc::smem_u32(pa_full), peer);
-            if (tc::mbar_wait(a_full, 0, a.err, 8)) {
-                tc::mbar_arrive_cluster(r_pa);
-                for (int st = 0; st < steps; ++st) {
-                    const int s = st % KST;
-                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 9)) break;
-                    tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(&pfull[s]), peer));
-                }
-            }
+            // the odd CTA tells the even CTA that its query tile landed
+            if (tc::mbar_wait(a_full, 0, a.err, 8)) tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(pa_full), peer));
         } else if (lane == 0) {
             // the even CTA issues the pair MMAs
             constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * TILE, WIDE);
@@ -896,8 +931,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1) 
                 for (int kb = 0; ok && kb < kblocks; ++kb) {
                     const int st = u * kblocks + kb;
                     const int s = st % KST;
-                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 4) ||
-                        !tc::mbar_wait(&pfull[s], (st / KST) & 1, a.err, 4)) { ok = false; break; }
+                    if (!tc::mbar_wait(&full[s], (st / KST) & 1, a.err, 4)) { ok = false; break; }
                     tc::tc_fence_after();
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {  // two K = 16 steps per 32-element K-block
@@ -1004,13 +1038,16 @@ cudaError_t launch_pair_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *l
     auto kern = tc_pair_kernel<KST, MC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
+    CUtensorMap dmap;
+    e = database_line_map(a, &dmap);
+    if (e != cudaSuccess) return e;
     const int64_t qtiles = ((a.m + TILE - 1) / TILE + 1) / 2 * 2;
     const int64_t per = wave > 0 ? (wave + 1) / 2 * 2 : qtiles;
     for (int64_t t0 = 0; t0 < qtiles; t0 += per) {
         TcArgs b = a;
         b.qt0 = t0;
         dim3 grid(unsigned(std::min<int64_t>(per, qtiles - t0)), unsigned(a.splits));
-        kern<<<grid, tc_threads<1>(), smem, st>>>(b);
+        kern<<<grid, tc_threads<1>(), smem, st>>>(b, dmap);
         if (launches) *launches += 1;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;

@@ -238,6 +238,20 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
 }
 
+// A 2D tiled TMA load into this CTA's shared memory whose completion
+// (complete_tx) is counted on an mbarrier that may belong to the peer CTA of
+// a CTA pair (`bar_cluster`: a shared::cluster address, e.g. from
+// mapa_shared).  Coordinates {x, y} in elements of the tensor map; x * the
+// element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d_pair(void *dst_smem, const void *tmap, int x, int y,
+                                                 uint32_t bar_cluster) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst_smem)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(bar_cluster), "r"(x), "r"(y)
+        : "memory");
+}
+
 // Every thread of both CTAs of the cluster.
 __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
