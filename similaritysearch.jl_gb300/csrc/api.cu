@@ -117,6 +117,10 @@ struct ssg_index {
     // ps_rows rows; the current queries' tiles (ps_q)
     DevBuf ps_db, ps_dbq, ps_norm, ps_q;
     int64_t ps_rows = -1, ps_qrows = -1;
+    // the same for wide vectors in the K-streaming layout: split tiles of the
+    // database (both roles), its epilogue coefficients, the queries' tiles
+    DevBuf pss_db, pss_dbq, pss_alpha, pss_beta, pss_q;
+    int64_t pss_rows = -1, pss_qrows = -1;
     int plain_tc_param = 1;
     int last_plain_tc = 0;  // 1: the last plain-method search ran on the tensor cores
     int64_t smp_r = 0, smp_n = -1, smp_rows = 0;
@@ -759,9 +763,25 @@ PlainTcPlan plain_tc_plan(const ssg_index *idx, int take) {
     return {};
 }
 
+// max |x|^2 over the database for the dot metrics' completeness check (the
+// squared-distance metrics keep it current on every append).
+int ensure_max_norm(ssg_index *idx) {
+    if (is_sq_metric(idx->metric)) return SSG_OK;
+    SSG_CK(idx->sq_norm.ensure(size_t(idx->n) * 4), "allocating squared norms");
+    SSG_CK(idx->sq_max.ensure(16), "allocating the norm maximum");
+    SSG_CK(cudaMemsetAsync(idx->sq_max.p, 0, 4, idx->stream), "clearing the norm maximum");
+    SSG_CK(ssg::launch_row_sq_norms(static_cast<const float *>(idx->db.p), idx->n, idx->dim,
+                                    static_cast<float *>(idx->sq_norm.p), static_cast<float *>(idx->sq_max.p),
+                                    idx->stream, &idx->last_launches),
+           "computing squared norms");
+    SSG_CK(cudaMemcpyAsync(&idx->max_x_sq, idx->sq_max.p, 4, cudaMemcpyDeviceToHost, idx->stream),
+           "reading the norm maximum");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "computing squared norms");
+    return SSG_OK;
+}
+
 // Two-piece tiles of the database (database role; the query role as well for
-// allknn), |x|^2 per padded row, and max |x|^2 for the dot metrics' check
-// (the squared-distance metrics keep it current on every append).
+// allknn), |x|^2 per padded row, and max |x|^2 for the dot metrics' check.
 int ensure_plain_tiles(ssg_index *idx, bool query_role) {
     const int64_t tiles = (ssg::tc_tiles(idx->n) + 1) / 2 * 2;
     const size_t tb = ssg::tc_tile_bytes(3 * ssg::tc_padded_k(idx->dim));
@@ -776,16 +796,7 @@ int ensure_plain_tiles(ssg_index *idx, bool query_role) {
         SSG_CK(ssg::launch_tc_norms(SSG_METRIC_SQL2, x, idx->n, idx->dim, tiles * 128,
                                     static_cast<float *>(idx->ps_norm.p), idx->stream, &idx->last_launches),
                "computing split tile norms");
-        if (!is_sq_metric(idx->metric)) {
-            SSG_CK(idx->sq_norm.ensure(size_t(idx->n) * 4), "allocating squared norms");
-            SSG_CK(idx->sq_max.ensure(16), "allocating the norm maximum");
-            SSG_CK(cudaMemsetAsync(idx->sq_max.p, 0, 4, idx->stream), "clearing the norm maximum");
-            SSG_CK(ssg::launch_row_sq_norms(x, idx->n, idx->dim, static_cast<float *>(idx->sq_norm.p),
-                                            static_cast<float *>(idx->sq_max.p), idx->stream, &idx->last_launches),
-                   "computing squared norms");
-            SSG_CK(cudaMemcpyAsync(&idx->max_x_sq, idx->sq_max.p, 4, cudaMemcpyDeviceToHost, idx->stream),
-                   "reading the norm maximum");
-        }
+        SSG_RC(ensure_max_norm(idx));
         SSG_CK(cudaStreamSynchronize(idx->stream), "building split database tiles");
         idx->ps_rows = idx->n;
     }
@@ -914,6 +925,145 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
     return run_fallback(idx, dq, m, k, exclude_self, flags, nflag, d_ids, d_dists);
 }
 
+// The plain method on the tensor cores for wide vectors (dim > 128, where a
+// resident split query tile does not fit): the same two-piece split and
+// certificate through the K-streaming scan, both operands streamed along
+// K = 3 kp (kp = dim padded to 64).  Returns SSG_OK, an error, or
+// kPlainNotApplicable when the list does not fit the scan's heaps.
+constexpr int kPlainNotApplicable = 1;
+
+int ensure_plain_stream_tiles(ssg_index *idx, bool query_role) {
+    const int64_t tiles = ssg::tc_tiles(idx->n);
+    const float *x = static_cast<const float *>(idx->db.p);
+    const size_t tb = 3 * ssg::stream_tile_bytes(idx->dim, 0);
+    if (idx->pss_rows != idx->n) {
+        idx->pss_qrows = -1;
+        SSG_CK(idx->pss_db.ensure(size_t(tiles) * tb), "allocating split database tiles");
+        SSG_CK(ssg::launch_stream_tiles(x, idx->n, idx->dim, 0, tiles, static_cast<uint8_t *>(idx->pss_db.p),
+                                        nullptr, idx->stream, &idx->last_launches, 1),
+               "building split database tiles");
+        SSG_CK(idx->pss_alpha.ensure(size_t(tiles) * 128 * 4), "allocating epilogue coefficients");
+        SSG_CK(idx->pss_beta.ensure(size_t(tiles) * 128 * 4), "allocating epilogue coefficients");
+        SSG_CK(ssg::launch_stream_coefs(idx->metric, x, idx->n, idx->dim, tiles * 128, nullptr,
+                                        static_cast<float *>(idx->pss_alpha.p), static_cast<float *>(idx->pss_beta.p),
+                                        idx->stream, &idx->last_launches),
+               "computing epilogue coefficients");
+        SSG_RC(ensure_max_norm(idx));
+        SSG_CK(cudaStreamSynchronize(idx->stream), "building split database tiles");
+        idx->pss_rows = idx->n;
+    }
+    if (query_role && idx->pss_qrows != idx->n) {
+        SSG_CK(idx->pss_dbq.ensure(size_t(tiles) * tb), "allocating split query-role tiles");
+        SSG_CK(ssg::launch_stream_tiles(x, idx->n, idx->dim, 0, tiles, static_cast<uint8_t *>(idx->pss_dbq.p),
+                                        nullptr, idx->stream, &idx->last_launches, 2),
+               "building split query-role tiles");
+        idx->pss_qrows = idx->n;
+    }
+    return SSG_OK;
+}
+
+int run_plain_stream(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
+                     float *d_dists, bool queries_are_db) {
+    const int metric = idx->metric;
+    if (metric != SSG_METRIC_SQL2 && metric != SSG_METRIC_L2 && metric != SSG_METRIC_NORMCOSINE &&
+        metric != SSG_METRIC_IP)
+        return kPlainNotApplicable;
+    const bool sq = is_sq_metric(metric);
+    const int take = k + (exclude_self ? 1 : 0);
+    const int margin = idx->margin_param > 0 ? idx->margin_param : std::max(8, (9 * take + 19) / 20);
+    const int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
+    const int heap_rows = ssg::stream_heap_rows(m);
+    int cs = 0, stages = 0;
+    if (!ssg::stream_choose(kk, heap_rows, &cs, &stages)) return kPlainNotApplicable;
+    const int kp = ssg::stream_kbytes(idx->dim, 0) / 2;  // elements per piece
+    const int64_t k3 = 3 * int64_t(kp);
+    SSG_RC(ensure_plain_stream_tiles(idx, queries_are_db));
+    const int64_t qtiles = (m + 127) / 128;
+    const int64_t n_tiles = ssg::tc_tiles(idx->n);
+    int64_t splits = idx->splits_param > 0 ? idx->splits_param : wave_splits(qtiles, ssg::device_sm_count(), n_tiles);
+    splits = std::max<int64_t>(1, std::min<int64_t>(splits, n_tiles));
+    const int segs = int(splits) * cs;
+    const size_t per_query = size_t(segs) * kk * 8;
+    int64_t chunk = std::max<int64_t>(128, int64_t((size_t(1) << 30) / per_query) / 128 * 128);
+    chunk = std::min<int64_t>(chunk, qtiles * 128);
+    SSG_CK(idx->cand.ensure(per_query * size_t(chunk)), "allocating candidate scratch");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    SSG_CK(idx->flags.ensure(size_t(m) * 4 + 16), "allocating query flags");
+    SSG_CK(cudaMemsetAsync(idx->flags.p, 0, size_t(m) * 4 + 16, idx->stream), "clearing query flags");
+    SSG_CK(idx->qsq.ensure(size_t(chunk) * 4 + 16), "allocating query norms");
+    const size_t tb = 3 * ssg::stream_tile_bytes(idx->dim, 0);
+    const uint8_t *qt = static_cast<const uint8_t *>(idx->pss_dbq.p);
+    if (!queries_are_db) {
+        SSG_CK(idx->pss_q.ensure(size_t(qtiles) * tb), "allocating split query tiles");
+        SSG_CK(ssg::launch_stream_tiles(dq, m, idx->dim, 0, qtiles, static_cast<uint8_t *>(idx->pss_q.p), nullptr,
+                                        idx->stream, &idx->last_launches, 2),
+               "building split query tiles");
+        qt = static_cast<const uint8_t *>(idx->pss_q.p);
+    }
+    // the K-streaming scan's shared pruning bounds, as for its reduced-precision use
+    uint32_t *gbound = nullptr;
+    if (kk >= 32 && 2 * splits * cs >= kk) {
+        SSG_CK(idx->gbound.ensure(size_t(chunk) * ssg::kBoundWords * 4), "allocating query bounds");
+        gbound = static_cast<uint32_t *>(idx->gbound.p);
+    }
+    // the error bound of the split (run_plain_tc) with this kp
+    const float c = 3.05f * 1.52587890625e-5f + 2.2f * float(kp) * 1.1920929e-7f;
+    const float ulp24 = 5.9604645e-8f;
+    int *flags = static_cast<int *>(idx->flags.p);
+    int *flag_count = flags + m;
+    float *qsq = static_cast<float *>(idx->qsq.p);
+    ScanTimer timer(idx);
+    for (int64_t c0 = 0; c0 < m; c0 += chunk) {
+        const int64_t mc = std::min<int64_t>(chunk, m - c0);
+        if (gbound)
+            SSG_CK(cudaMemsetAsync(gbound, 0, size_t(mc) * ssg::kBoundWords * 4, idx->stream),
+                   "clearing query bounds");
+        SSG_RC(timer.begin());
+        SSG_CK(ssg::launch_stream_scan(qt + size_t(c0 / 128) * tb, static_cast<const uint8_t *>(idx->pss_db.p),
+                                       static_cast<const float *>(idx->pss_alpha.p),
+                                       static_cast<const float *>(idx->pss_beta.p), nullptr, idx->n, mc, k3, 0, kk,
+                                       int(splits), heap_rows, gbound, static_cast<uint64_t *>(idx->cand.p),
+                                       static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr),
+               "launching the split streaming scan");
+        SSG_RC(timer.end());
+        const float *qc = dq + size_t(c0) * idx->dim;
+        SSG_CK(ssg::launch_row_sq_norms(qc, mc, idx->dim, qsq, qsq + chunk, idx->stream, &idx->last_launches),
+               "computing query norms");
+        ssg::FinalizeArgs f{};
+        SSG_RC(reduce_segments(idx, static_cast<const uint64_t *>(idx->cand.p), mc, segs, kk, &f.cand, &f.segs));
+        f.kk = kk;
+        f.m = mc;
+        f.k_out = k;
+        f.exclude_self = exclude_self;
+        f.self_base = c0;
+        f.out_ids = d_ids + size_t(c0) * k;
+        f.out_dists = d_dists + size_t(c0) * k;
+        f.n_rows = idx->n;
+        f.check = sq ? 1 : 2;
+        f.q_sq = qsq;
+        f.max_x_sq = idx->max_x_sq;
+        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c : c + float(idx->dim + 2) * ulp24;
+        f.n_total = idx->n;
+        f.flags = flags + c0;
+        f.flag_count = flag_count;
+        SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc, nullptr,
+                                           idx->stream, &idx->last_launches),
+               "launching the rerank kernel");
+        SSG_RC(timer.collect());
+    }
+    int status = 0, nflag = 0;
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaMemcpyAsync(&nflag, flag_count, sizeof(int), cudaMemcpyDeviceToHost, idx->stream), "reading flags");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "running the split streaming scan");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the split streaming scan gave up (code %d)", status);
+    idx->last_fallbacks = nflag;
+    return run_fallback(idx, dq, m, k, exclude_self, flags, nflag, d_ids, d_dists);
+}
+
 int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                uint32_t *d_ids, float *d_dists, bool queries_are_db);
 int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
@@ -941,6 +1091,14 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
         if (plan.k3 > 0)
             return run_plain_tc(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
                                 queries_are_db, plan);
+        if (ssg::tc_padded_k(idx->dim) > 128) {
+            const int rc = run_plain_stream(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
+                                            queries_are_db);
+            if (rc != kPlainNotApplicable) {
+                idx->last_plain_tc = rc == SSG_OK;
+                return rc;
+            }
+        }
     }
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
         const int take = k + (exclude_self ? 1 : 0);
@@ -2253,7 +2411,8 @@ void ssg_destroy(ssg_index *idx) {
     for (DevBuf *b : {&idx->sq_norm, &idx->sq_max, &idx->flags, &idx->qsq, &idx->fb_list, &idx->fb_q, &idx->fb_out,
                       &idx->fb_cand, &idx->fb_qn, &idx->tc_smp, &idx->tc_smp_norm, &idx->f_out, &idx->f_cnt,
                       &idx->f_thr, &idx->gbound, &idx->pack_q, &idx->pack_out, &idx->gm_db, &idx->gm_q,
-                      &idx->ps_db, &idx->ps_dbq, &idx->ps_norm, &idx->ps_q, &idx->qbound})
+                      &idx->ps_db, &idx->ps_dbq, &idx->ps_norm, &idx->ps_q, &idx->qbound, &idx->pss_db,
+                      &idx->pss_dbq, &idx->pss_alpha, &idx->pss_beta, &idx->pss_q})
         b->release();
     if (idx->ev0) cudaEventDestroy(idx->ev0);
     if (idx->ev1) cudaEventDestroy(idx->ev1);

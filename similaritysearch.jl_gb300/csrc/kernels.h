@@ -175,9 +175,11 @@ size_t stream_tile_bytes(int64_t dim, int fp8);   // bytes per 128-row tile
 constexpr int kBoundWords = 16;                   // shared pruning-bound words per query
 int stream_heap_rows(int64_t m);                  // query rows of a tile that own heaps
 bool stream_choose(int kk, int heap_rows, int *cs, int *stages);
-// rows -> K-block tiles; FP8 also writes the per-row scale (scale may be null for BF16)
+// rows -> K-block tiles; FP8 also writes the per-row scale (scale may be null
+// for BF16).  split 1 / 2 (BF16): the plain method's two-piece tiles, K = 3 x
+// the padded dim, database / query layout (tc_stream.cu)
 cudaError_t launch_stream_tiles(const float *x, int64_t rows, int64_t dim, int fp8, int64_t tiles, uint8_t *out,
-                                float *scale, cudaStream_t st, int *launches);
+                                float *scale, cudaStream_t st, int *launches, int split = 0);
 // per padded database row: alpha / beta of the approximate distance
 cudaError_t launch_stream_coefs(int metric, const float *x, int64_t rows, int64_t dim, int64_t padded,
                                 const float *scale, float *alpha, float *beta, cudaStream_t st, int *launches);

@@ -50,8 +50,12 @@ __host__ __device__ constexpr int st_threads() { return 64 + TILE * CS; }
 // Prep: rows -> swizzled K-block tiles (BF16 or scaled FP8) + per-row scale.
 // One warp per row.
 // ---------------------------------------------------------------------------
+// split != 0 (BF16 only): the plain method's two-piece form, three segments
+// of kp = kbytes / 6 elements along K, database rows (split 1) as
+// [lo | hi | hi] and query rows (split 2) as [hi | lo | hi], with
+// hi = bf16(x) and lo = bf16(x - hi) (see tc_bf16.cu, bf16_tile_kernel).
 __global__ void stream_tile_kernel(const float *__restrict__ x, int64_t rows, int dim, int kbytes, int fp8,
-                                   int64_t tiles, uint8_t *__restrict__ out, float *__restrict__ scale) {
+                                   int split, int64_t tiles, uint8_t *__restrict__ out, float *__restrict__ scale) {
     const int lane = threadIdx.x % 32;
     const int64_t wid = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
     const int64_t nw = int64_t(gridDim.x) * blockDim.x / 32;
@@ -82,6 +86,17 @@ __global__ void stream_tile_kernel(const float *__restrict__ x, int64_t rows, in
                 for (int e = 0; e < 16; ++e) {
                     const float f = (valid && e0 + e < dim) ? xr[e0 + e] * inv : 0.0f;
                     buf[e] = __nv_cvt_float_to_fp8(f, __NV_SATFINITE, __NV_E4M3);
+                }
+            } else if (split) {
+                const int kp = kbytes / 6;
+                const int seg = e0 / kp, scol = e0 % kp;
+                const bool low = (split == 1 && seg == 0) || (split == 2 && seg == 1);
+                __nv_bfloat16 *b = reinterpret_cast<__nv_bfloat16 *>(buf);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const float f = (valid && scol + e < dim) ? xr[scol + e] : 0.0f;
+                    const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+                    b[e] = low ? __float2bfloat16_rn(f - __bfloat162float(hi)) : hi;
                 }
             } else {
                 __nv_bfloat16 *b = reinterpret_cast<__nv_bfloat16 *>(buf);
@@ -479,14 +494,15 @@ bool stream_choose(int kk, int heap_rows, int *cs, int *stages) {
 }
 
 cudaError_t launch_stream_tiles(const float *x, int64_t rows, int64_t dim, int fp8, int64_t tiles, uint8_t *out,
-                                float *scale, cudaStream_t st, int *launches) {
+                                float *scale, cudaStream_t st, int *launches, int split) {
+    if (split && fp8) return cudaErrorInvalidValue;
     const int64_t warps = tiles * TILE;
     int64_t blocks = (warps * 32 + 255) / 256;
     if (blocks > 148 * 32) blocks = 148 * 32;
     if (blocks < 1) blocks = 1;
     if (launches) *launches += 1;
-    stream_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), stream_kbytes(dim, fp8), fp8, tiles,
-                                                          out, scale);
+    const int kbytes = (split ? 3 : 1) * stream_kbytes(dim, fp8);
+    stream_tile_kernel<<<unsigned(blocks), 256, 0, st>>>(x, rows, int(dim), kbytes, fp8, split, tiles, out, scale);
     return cudaGetLastError();
 }
 

@@ -59,6 +59,21 @@ def test_plain_tc_searchbatch_bitexact(ss, name, d, k, on_tc):
     assert np.array_equal(gi, ci) and np.array_equal(gd, cd)
 
 
+@pytest.mark.parametrize("name", list(METRICS))
+@pytest.mark.parametrize("d,k", [(200, 10), (768, 1), (768, 20), (300, 33)])
+def test_plain_tc_streaming_wide_vectors_bitexact(ss, name, d, k):
+    """dim > 128: the split tiles stream along K = 3 kp through the K-streaming
+    scan; same certificate, same exact results."""
+    X, Q = make(name, 12000, 200, d, seed=d + k)
+    gi, gd, idx = run(ss, name, X, Q, k)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.searchbatch(name, X, Q, k, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri)
+    assert np.array_equal(gd, rd)
+    ci, cd, cidx = run(ss, name, X, Q, k, plain_tc=0)
+    assert np.array_equal(gi, ci) and np.array_equal(gd, cd)
+
+
 @pytest.mark.parametrize("name", ["sql2", "normcosine"])
 def test_plain_tc_allknn_bitexact(ss, name):
     rng = np.random.default_rng(61)
