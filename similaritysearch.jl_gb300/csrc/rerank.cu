@@ -117,7 +117,12 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         // FP32 distance D(y) >= a(y) + c - E, where c turns keys into
         // distances and E bounds the approximation and evaluation errors:
         //   check 1 (keys |x|^2 - 2 x.q of SqL2 / L2): c = |q|^2,
-        //           E = err_scale (sqrt(max |x|^2) + |q|)^2;
+        //           E = err_scale (R + |q|)^2, R a bound on |y| for every y
+        //           that could rank at or before the take-th candidate:
+        //           |y - q|^2 <= D_take (up to the FP32 evaluation's relative
+        //           error t^2 = (d + 2) 2^-24 of (|y| + |q|)^2) gives
+        //           |y| <= ((1 + t) |q| + sqrt(D_take)) / (1 - t), and
+        //           |y| <= sqrt(max |x|^2) always;
         //   check 2 (keys -x.q): c = 1 for NormCosine, 0 for InnerProduct,
         //           E = err_scale sqrt(max |x|^2) |q| + 2^-22.
         // If a_low + c - E exceeds the exact distance of the take-th
@@ -144,9 +149,14 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
                 c = METRIC == NORMCOSINE ? 1.0 : 0.0;
                 E = double(f.err_scale) * xm * sqrt(qs) + 2.384185791015625e-7;
             }
-            const double lower = double(key_dist(low)) + c - E;
             double dtake = double(key_dist(s2[take - 1]));
             if (METRIC == L2) dtake = dtake * dtake * (1.0 + 9.5367431640625e-7);
+            if (f.check == 1 && dtake >= 0.0) {
+                const double t = sqrt(double(dim + 2) * 5.9604644775390625e-8);
+                const double r = fmin(xm, ((1.0 + t) * sqrt(qs) + sqrt(dtake)) / (1.0 - t)) + sqrt(qs);
+                E = double(f.err_scale) * r * r;
+            }
+            const double lower = double(key_dist(low)) + c - E;
             if (!(lower > dtake)) {
                 f.flags[j] = 1;
                 atomicAdd(f.flag_count, 1);
