@@ -728,11 +728,23 @@ int run_fallback(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
 // exact direct scan, so the result is the plain method's, bit for bit.
 // ---------------------------------------------------------------------------
 
+// Candidates kept beyond the k + self needed by the plain method's scans:
+// 0.45 k, at least 8, and for the squared distances at least dim / 12 (their
+// error bound grows with dim times the squared norms, so wide vectors need a
+// longer list to certify a query: at 768 dimensions and k = 10, 8 extra
+// candidates left two thirds of C4's queries uncertified).
+int plain_margin(const ssg_index *idx, int take) {
+    if (idx->margin_param > 0) return idx->margin_param;
+    int mg = std::max(8, (9 * take + 19) / 20);
+    if (is_sq_metric(idx->metric)) mg = std::max<int>(mg, int(idx->dim / 12));
+    return mg;
+}
+
 // How the plain method runs on the tensor cores: split K (0: it does not
 // apply -- metric, dimension, or no scan kernel holds the tiles and the
 // heaps), candidates kept per heap and candidates re-ranked per query.  The
-// list is k + margin long (margin 0.45 k, at least 8: a fallback costs far
-// more than a longer list).  Each heap keeps the whole list when the one-CTA
+// list is k + plain_margin long (a fallback costs far more than a longer
+// list).  Each heap keeps the whole list when the one-CTA
 // wide scan holds it with four ring stages or more.  Otherwise each of a
 // query tile's two column heaps keeps part of it, as many as fit beside four
 // ring stages and at least half the list: the completeness check then stops
@@ -750,7 +762,7 @@ PlainTcPlan plain_tc_plan(const ssg_index *idx, int take) {
         return {};
     const int k3 = 3 * ssg::tc_padded_k(idx->dim);
     if (k3 > 384) return {};
-    const int margin = idx->margin_param > 0 ? idx->margin_param : std::max(8, (9 * take + 19) / 20);
+    const int margin = plain_margin(idx, take);
     const int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
     if (ssg::tc_wide_stages(k3, kk) >= 4) return {k3, kk, kk};
     int h = (kk + 1) / 2;
@@ -970,10 +982,14 @@ int run_plain_stream(ssg_index *idx, const float *dq, int64_t m, int k, int excl
         return kPlainNotApplicable;
     const bool sq = is_sq_metric(metric);
     const int take = k + (exclude_self ? 1 : 0);
-    const int margin = idx->margin_param > 0 ? idx->margin_param : std::max(8, (9 * take + 19) / 20);
-    const int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
+    // the margin shrinks (down to the list's basic 0.45 k) until the scan's heaps hold it
+    const int margin = plain_margin(idx, take);
+    const int base = std::min(margin, std::max(8, (9 * take + 19) / 20));
+    int kk = int(std::min<int64_t>(int64_t(take) + margin, idx->n));
+    const int kk_min = int(std::min<int64_t>(int64_t(take) + base, idx->n));
     const int heap_rows = ssg::stream_heap_rows(m);
     int cs = 0, stages = 0;
+    while (kk > kk_min && !ssg::stream_choose(kk, heap_rows, &cs, &stages)) --kk;
     if (!ssg::stream_choose(kk, heap_rows, &cs, &stages)) return kPlainNotApplicable;
     const int kp = ssg::stream_kbytes(idx->dim, 0) / 2;  // elements per piece
     const int64_t k3 = 3 * int64_t(kp);
@@ -1103,6 +1119,9 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
         const int take = k + (exclude_self ? 1 : 0);
         int64_t kk = is_sq_metric(idx->metric) ? int64_t(take) + gemm_margin(idx, take) : take;
+        // the longer list of the tensor-core forms where the heaps hold it
+        if (is_sq_metric(idx->metric) && ssg::gemm_fits(int(take + plain_margin(idx, take))))
+            kk = int64_t(take) + plain_margin(idx, take);
         kk = std::min<int64_t>(kk, std::max<int64_t>(1, idx->n));
         if (ssg::gemm_fits(int(kk)))
             return run_gemm(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists, int(kk));
