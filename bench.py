@@ -830,6 +830,11 @@ def suite_c4(cx, args, data):
         lat_w, res_w, calls = c4_windows(cx, h, Qd, sizes, ks, offs, d, window)
         replays = int(cx.get(h, "graph_replays") - r0)
         lat_p, res_p = c4_stream(cx, h, Qd, sizes, ks, offs, d, True)
+        # the same plain method on the CUDA cores (identical results)
+        cx.set(h, "plain_tc", 0.0)
+        lat_pc, res_pc = c4_stream(cx, h, Qd, sizes, ks, offs, d, True)
+        cx.set(h, "plain_tc", 1.0)
+        plain_same = all(np.array_equal(a, b) for a, b in zip(res_p, res_pc))
         big = [b for b in range(len(sizes)) if ks[b] >= 10]
         wts = sizes[big].astype(np.float64)
         rec = float(np.average([O.macrorecall(res_p[b][:, :10], res_r[b][:, :10]) for b in big], weights=wts))
@@ -879,6 +884,13 @@ def suite_c4(cx, args, data):
             "plain_fp32": {"value": tq / lat_p.sum(), "latency_ms": {"p50": float(np.percentile(lat_p, 50) * 1e3),
                                                                      "p99": float(np.percentile(lat_p, 99) * 1e3)}},
             "speedup_vs_plain": float(lat_p.sum() / lat_r.sum()),
+            "plain_fp32_cuda_cores": {"value": tq / lat_pc.sum(),
+                                      "latency_ms": {"p50": float(np.percentile(lat_pc, 50) * 1e3),
+                                                     "p99": float(np.percentile(lat_pc, 99) * 1e3)},
+                                      "ids_equal_to_plain_fp32": plain_same,
+                                      "note": "plain_fp32 runs on the tensor cores (two-piece BF16, certified "
+                                              "exact); this is the same method on the CUDA cores"},
+            "speedup_vs_plain_cuda_cores": float(lat_pc.sum() / lat_r.sum()),
             "coalesced": {"window_batches": window, "value": tq / lat_w.sum(), "unit": "queries/s",
                           "latency_ms_per_window": {"p50": float(np.percentile(lat_w, 50) * 1e3),
                                                     "p99": float(np.percentile(lat_w, 99) * 1e3)},
@@ -936,6 +948,10 @@ def suite_c5(cx, args, data):
     steps, warmup = max(3, args.steps // 2), max(3, args.warmup)
     qps_plain, ms_plain, gold = timed(steps, warmup)
     gold_h = heldout()
+    # the same plain method on the CUDA cores (identical results)
+    cx.set(h, "plain_tc", 0.0)
+    qps_plain_cc, ms_plain_cc, gold_cc = timed(1, 1)
+    cx.set(h, "plain_tc", 1.0)
     ladder = (512, 256, 128, 64, 32)
 
     def sweep(tag):
@@ -1005,7 +1021,11 @@ def suite_c5(cx, args, data):
             "recall@10_vs_fp64_heldout": {"learned": O.macrorecall(fi, got_h[:ns]),
                                           "plain": O.macrorecall(fi, gold_h[:ns]), "queries": ns},
             "heldout_recall_by_shortlist": tr_rows, "training": stats, "random_projection": rp,
-            "plain_fp32": {"value": qps_plain, "ms_per_step": ms_plain},
+            "plain_fp32": {"value": qps_plain, "ms_per_step": ms_plain,
+                           "note": "two-piece BF16 on the tensor cores, certified exact"},
+            "plain_fp32_cuda_cores": {"value": qps_plain_cc, "ms_per_step": ms_plain_cc,
+                                      "ids_equal_to_plain_fp32": bool(np.array_equal(gold, gold_cc))},
+            "speedup_vs_plain_cuda_cores": qps_l / qps_plain_cc,
             "speedup_vs_plain": qps_l / qps_plain, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": m / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(Qs.nbytes),
                     "d2h_bytes_per_step": int(m * k * 8)},
