@@ -154,3 +154,18 @@ def test_plain_tc_allknn_locality_order(ss, name):
         keep = [t for t in range(17) if ri[r, t] != j + 1][:16]
         assert np.array_equal(ids.T[j], ri[r, keep])
         assert np.array_equal(dists.T[j], rd[r, keep])
+
+
+@pytest.mark.parametrize("name", ["sql2", "normcosine"])
+def test_plain_tc_on_cta_pairs_bitexact(ss, name):
+    """The split scan on CTA pairs (M = 256 MMAs, the odd CTA's half of each
+    K-block counted on the even CTA's barrier) answers the same."""
+    X, Q = make(name, 20000, 333, 96, seed=71)
+    gi, gd, idx = run(ss, name, X, Q, 32)
+    idx2 = ss.GPUExhaustiveSearch(getattr(ss.Dist, METRICS[name])(), ss.MatrixDatabase.from_rows(X))
+    idx2.set_param("pair", 1)
+    pi, pd = ss.searchbatch(idx2, ss.GenericContext(logger=None), ss.MatrixDatabase.from_rows(Q), 32)
+    assert idx2.get_param("last_plain_tc") == 1.0
+    assert np.array_equal(pi.T, gi) and np.array_equal(pd.T, gd)
+    ri, rd = O.searchbatch(name, X, Q, 32, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
