@@ -169,3 +169,36 @@ def test_plain_tc_on_cta_pairs_bitexact(ss, name):
     assert np.array_equal(pi.T, gi) and np.array_equal(pd.T, gd)
     ri, rd = O.searchbatch(name, X, Q, 32, lanes=1, nthreads=O.num_threads())
     assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
+@pytest.mark.parametrize("m", [1, 129])
+@pytest.mark.parametrize("d", [17, 160])
+def test_plain_tc_edge_shapes(ss, m, d):
+    """The smallest database the tensor-core form takes (4,096 rows), a single
+    query and a query count one past a tile, dims off the padding grid."""
+    X, Q = make("sql2", 4096, m, d, seed=m * 1000 + d)
+    gi, gd, idx = run(ss, "sql2", X, Q, 7)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.searchbatch("sql2", X, Q, 7, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
+
+
+def test_plain_tc_allknn_with_duplicate_rows(ss):
+    """allknn excluding self over rows that come in identical pairs: the
+    twin sits at distance 0 and self is dropped by id, in (distance, id)
+    order, as the reference's KnnSorted gives."""
+    rng = np.random.default_rng(65)
+    base = rng.standard_normal((2100, 40), dtype=np.float32)
+    X = np.repeat(base, 2, axis=0)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X))
+    ids, dists = ss.allknn(idx, ss.GenericContext(logger=None), 5, exclude_self=True)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.allknn("sql2", X, 6, lanes=1, nthreads=O.num_threads())
+    for j in range(0, X.shape[0], 97):
+        keep = [t for t in range(6) if ri[j, t] != j + 1][:5]
+        assert np.array_equal(ids.T[j], ri[j, keep])
+        assert np.array_equal(dists.T[j], rd[j, keep])
+    # every row's nearest neighbour is its twin at distance 0
+    twin = np.arange(X.shape[0]) ^ 1
+    assert np.array_equal(ids[0], (twin + 1).astype(np.uint32))
+    assert np.all(dists[0] == 0)
