@@ -129,15 +129,20 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         // re-ranked candidate (for L2 its square, widened by 2^-20 so that
         // sqrt rounding cannot tie), y ranks behind it: the list holds the
         // exact top `take`.  Evaluated in double.
+        // A list shorter than rr (heaps that a shared bound kept from
+        // filling) holds every candidate no heap dropped: a_low is then the
+        // full segments' smallest last key alone.  A list that holds every
+        // row needs no check; one shorter than `take` cannot be certified.
         const int take = f.k_out + (f.exclude_self ? 1 : 0);
         int nv = 0;
         while (nv < rr && s1[nv] != KEY_EMPTY) ++nv;
-        if (nv == rr && int64_t(rr) < f.n_total && take <= rr) {
-            uint64_t low = s1[rr - 1];
+        if (int64_t(nv) < f.n_total) {
+            uint64_t low = nv == rr ? s1[rr - 1] : KEY_EMPTY;
             for (int sgi = 0; sgi < f.segs; ++sgi) {
                 const uint64_t last = src[size_t(sgi) * f.kk + f.kk - 1];
                 if (last != KEY_EMPTY && last < low) low = last;
             }
+            bool certified = nv >= take && low != KEY_EMPTY;
             const double qs = double(f.q_sq[j]);
             const double xm = sqrt(double(f.max_x_sq));
             double c, E;
@@ -149,15 +154,15 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
                 c = METRIC == NORMCOSINE ? 1.0 : 0.0;
                 E = double(f.err_scale) * xm * sqrt(qs) + 2.384185791015625e-7;
             }
-            double dtake = double(key_dist(s2[take - 1]));
+            double dtake = certified ? double(key_dist(s2[take - 1])) : 0.0;
             if (METRIC == L2) dtake = dtake * dtake * (1.0 + 9.5367431640625e-7);
             if (f.check == 1 && dtake >= 0.0) {
                 const double t = sqrt(double(dim + 2) * 5.9604644775390625e-8);
                 const double r = fmin(xm, ((1.0 + t) * sqrt(qs) + sqrt(dtake)) / (1.0 - t)) + sqrt(qs);
                 E = double(f.err_scale) * r * r;
             }
-            const double lower = double(key_dist(low)) + c - E;
-            if (!(lower > dtake)) {
+            const double lower = certified ? double(key_dist(low)) + c - E : 0.0;
+            if (!certified || !(lower > dtake)) {
                 f.flags[j] = 1;
                 atomicAdd(f.flag_count, 1);
             }
