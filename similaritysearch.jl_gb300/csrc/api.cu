@@ -874,8 +874,10 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
         perm = static_cast<const uint32_t *>(idx->loc_perm.p);
         rot = static_cast<const int *>(idx->loc_rot.p);
     }
+    // every heap of a query -- its splits and the two column halves of each
+    // CTA -- shares one bound (all ones: none yet)
     uint32_t *qbound = nullptr;
-    if (splits > 1) {
+    if (segs > 1) {
         SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
         qbound = static_cast<uint32_t *>(idx->qbound.p);
     }
@@ -1309,9 +1311,10 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
                "building BF16 query tiles");
         qtiles = static_cast<const uint8_t *>(idx->tc_q.p);
     }
-    // the splits of a query share one bound (all ones: none yet)
+    // every heap of a query -- its splits and the two column halves of each
+    // CTA -- shares one bound (all ones: none yet)
     uint32_t *qbound = nullptr;
-    if (splits > 1) {
+    if (segs > 1) {
         SSG_CK(idx->qbound.ensure(size_t(chunk) * 4), "allocating query bounds");
         qbound = static_cast<uint32_t *>(idx->qbound.p);
     }

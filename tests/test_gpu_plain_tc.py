@@ -202,3 +202,23 @@ def test_plain_tc_allknn_with_duplicate_rows(ss):
     twin = np.arange(X.shape[0]) ^ 1
     assert np.array_equal(ids[0], (twin + 1).astype(np.uint32))
     assert np.all(dists[0] == 0)
+
+
+@pytest.mark.parametrize("name", ["sql2", "normcosine"])
+def test_plain_tc_half_heaps_under_shared_bounds(ss, name):
+    """Rows stored cluster by cluster and a handful of queries: many database
+    splits per query, half-heaps that the shared bound keeps from filling;
+    the certificate must still hold (or fall back) -- results exact."""
+    rng = np.random.default_rng(66)
+    C = rng.standard_normal((40, 96), dtype=np.float32)
+    lab = np.sort(rng.integers(0, 40, 20000))
+    X = C[lab] + 0.2 * rng.standard_normal((20000, 96), dtype=np.float32)
+    if name == "normcosine":
+        X /= np.linalg.norm(X, axis=1, keepdims=True)
+    Q = X[rng.choice(20000, 37, replace=False)] + np.float32(1e-3)
+    if name == "normcosine":
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    gi, gd, idx = run(ss, name, X, Q, 32)
+    assert idx.get_param("last_plain_tc") == 1.0
+    ri, rd = O.searchbatch(name, X, Q, 32, lanes=1, nthreads=O.num_threads())
+    assert np.array_equal(gi, ri) and np.array_equal(gd, rd)
