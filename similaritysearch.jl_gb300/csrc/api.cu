@@ -96,6 +96,7 @@ struct ssg_index {
     int wide_param = 1;    // BF16 scan: 256-row database tiles per MMA
     int64_t wave_param = 0;  // wide scan: query tiles per launch (0: one launch)
     int pair_param = 0;      // wide scan on CTA pairs (M = 256 MMAs, half the database traffic per SM)
+    int long_param = 1;      // lists too long for two heaps per query: one heap per query on CTA pairs
     // K-streaming tensor-core path (FP8 mode, and BF16 for dim > 256): operand
     // tiles, per-row FP8 scales, per-row epilogue coefficients, query tiles
     DevBuf st_db, st_scale, st_alpha, st_beta, st_q, st_qscale;
@@ -1265,13 +1266,20 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     const int kp = ssg::tc_padded_k(idx->dim);
     int kk = int(kk64);
     int qt = 0, stages = 0;
+    bool long_lists = false;
     idx->last_fallbacks = 0;
-    // more candidates than the scans' on-chip heaps hold: threshold filter
-    // (the wide scan, one query tile per CTA, is chosen first when it fits)
+    // the wide scan (one query tile per CTA, two heaps per query) first when
+    // it fits; longer lists on CTA pairs with one heap per query (8 KB ring
+    // stages and one heap leave the list twice the room); beyond that the
+    // threshold filter
     const bool wide = idx->wide_param && (ssg::tc_wide_fits(kp, kk) || (idx->pair_param && ssg::tc_pair_fits(kp, kk)));
     if (wide) qt = 1;
-    else if (!ssg::tc_choose(kp, kk, &qt, &stages))
-        return run_knn_tc_filter(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db, kk);
+    else if (!ssg::tc_choose(kp, kk, &qt, &stages)) {
+        if (!(idx->wide_param && idx->long_param && ssg::tc_long_fits(kp, kk)))
+            return run_knn_tc_filter(idx, dq, dqn, m, k, exclude_self, d_ids, d_dists, queries_are_db, kk);
+        qt = 1;
+        long_lists = true;
+    }
     const int64_t qrows = int64_t(qt) * 128;
     const int64_t qctas = (m + qrows - 1) / qrows;
     const int64_t n_tiles = ssg::tc_tiles(idx->n);
@@ -1280,7 +1288,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
     splits = std::min<int64_t>(splits, n_tiles);
     splits = std::max<int64_t>(1, splits);
     // chunk the queries (a multiple of the CTA's query rows) to bound scratch
-    const int segs = int(splits) * ssg::tc_segments_per_split(qt);
+    const int segs = int(splits) * (long_lists ? 1 : ssg::tc_segments_per_split(qt));
     const size_t per_query = size_t(segs) * kk * 8;
     int64_t chunk = std::max<int64_t>(2 * qrows, int64_t((size_t(1) << 30) / per_query) / (2 * qrows) * (2 * qrows));
     chunk = std::min<int64_t>(chunk, (m + qrows - 1) / qrows * qrows);
@@ -1322,11 +1330,18 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
         const int64_t mc = std::min<int64_t>(chunk, m - c0);
         if (qbound) SSG_CK(cudaMemsetAsync(qbound, 0xff, size_t(mc) * 4, idx->stream), "clearing query bounds");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev0, idx->stream), "recording an event");
-        SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc, idx->dim,
-                                   kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
-                                   static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
-                                   perm, rot, idx->wide_param != 0, idx->wave_param, idx->pair_param != 0, qbound),
-               "launching the BF16 scan kernel");
+        if (long_lists)
+            SSG_CK(ssg::launch_tc_scan_long(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc,
+                                            idx->dim, kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
+                                            static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, perm,
+                                            rot, idx->wave_param, qbound),
+                   "launching the BF16 long-list scan kernel");
+        else
+            SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles + size_t(c0 / 128) * tb, dtiles, dnorm, idx->n, mc,
+                                       idx->dim, kk, int(splits), static_cast<uint64_t *>(idx->cand.p),
+                                       static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, nullptr,
+                                       perm, rot, idx->wide_param != 0, idx->wave_param, idx->pair_param != 0, qbound),
+                   "launching the BF16 scan kernel");
         if (idx->profile) SSG_CK(cudaEventRecord(idx->ev1, idx->stream), "recording an event");
         ssg::FinalizeArgs f{};
         SSG_RC(reduce_segments(idx, static_cast<const uint64_t *>(idx->cand.p), mc, segs, kk, &f.cand, &f.segs));
@@ -1738,7 +1753,7 @@ std::vector<uint64_t> graph_key(const ssg_index *idx, int64_t m, int k) {
     memcpy(&of, &idx->overfetch, 8);
     std::vector<uint64_t> key = {uint64_t(m), uint64_t(k), uint64_t(idx->n), uint64_t(idx->prec),
                                  uint64_t(idx->metric), of, uint64_t(idx->splits_param), uint64_t(idx->wide_param),
-                                 uint64_t(idx->wave_param), uint64_t(idx->pair_param)};
+                                 uint64_t(idx->wave_param), uint64_t(idx->pair_param), uint64_t(idx->long_param)};
     for (const DevBuf *b : {&idx->db, &idx->db_norm, &idx->tc_db, &idx->tc_norm, &idx->tc_q, &idx->st_db,
                             &idx->st_scale, &idx->st_alpha, &idx->st_beta, &idx->st_q, &idx->st_qscale, &idx->cand,
                             &idx->red[0], &idx->red[1], &idx->status, &idx->gbound, &idx->qnorm, &idx->pack_q,
@@ -2163,6 +2178,8 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->wide_param = value != 0.0;
     } else if (k == "pair") {
         idx->pair_param = value != 0.0;
+    } else if (k == "long_lists") {
+        idx->long_param = value != 0.0;
     } else if (k == "wave") {
         if (!(value >= 0 && value <= 1e6)) return fail(idx, SSG_EINVAL, "wave out of range");
         idx->wave_param = int64_t(value);
@@ -2200,6 +2217,7 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "exact_scan") *value = idx->exact_scan_param;
     else if (k == "plain") *value = idx->plain_param;
     else if (k == "plain_tc") *value = idx->plain_tc_param;
+    else if (k == "long_lists") *value = idx->long_param;
     else if (k == "last_plain_tc") *value = idx->last_plain_tc;
     else if (k == "learned") *value = idx->learned_param;
     else if (k == "learned_target") *value = idx->learned_target;

@@ -147,6 +147,14 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
                            cudaStream_t st, int *launches, int *qt_out, const uint32_t *perm = nullptr,
                            const int *rot = nullptr, bool wide = false, int64_t wave = 0, bool pair = false,
                            uint32_t *qbound = nullptr);
+// The same scan for candidate lists too long for the two heaps per query of
+// the wide and pair scans: CTA pairs with one heap per query (one segment per
+// split and query).  tc_long_fits tells whether kk fits.
+bool tc_long_fits(int kp, int kk);
+cudaError_t launch_tc_scan_long(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                                int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
+                                cudaStream_t st, int *launches, const uint32_t *perm, const int *rot, int64_t wave,
+                                uint32_t *qbound);
 // Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
 // segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
 // grouped by pivot) and rot (start tile of each query tile's scan).

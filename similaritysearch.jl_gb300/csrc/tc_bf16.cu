@@ -796,17 +796,20 @@ cudaError_t database_line_map(const TcArgs &a, CUtensorMap *map) {
 // ---------------------------------------------------------------------------
 constexpr int PKBLK = TILE * SW;  // one 128-row half of a wide K-block: 8 KB
 
-template <int KST>
+template <int KST, int CS = 2>
 struct PairSmem {
     static size_t total(int kp, int kk) {
-        return 1024 + size_t(TILE) * kp * 2 + size_t(KST) * PKBLK + TcSmem<1, 1>::heap_bytes(kk) + 512;
+        return 1024 + size_t(TILE) * kp * 2 + size_t(KST) * PKBLK + size_t(TILE) * CS * (kk + kBufCap) * 8 + 512;
     }
 };
 
-template <int KST, int MC>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1)
+// CS heaps per query: 2 (two epilogue warps per TMEM lane quarter, each
+// filtering one 128-column half of every wide tile into its own heap), or 1
+// (one warp per quarter filtering both halves into one heap: half the heap
+// memory, for candidate lists twice as long).
+template <int KST, int MC, int CS>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 + TILE * CS, 1)
     tc_pair_kernel(TcArgs a, const __grid_constant__ CUtensorMap dmap) {
-    constexpr int CS = 2;
     constexpr int NACC = 2;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -988,26 +991,33 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1)
             tc::tc_fence_after();
             T.refresh();
             constexpr int LDC = MC == MC_DOT ? 4 : 2;
-            const int64_t row0 = phys_wide(u) * WIDE + cs * TILE;
-            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * TILE);
             uint32_t r[LDC][32];
+            // this warp's column halves of the wide tile (one with two heaps
+            // per query, both with one); the accumulator goes back after the
+            // last load of the last half
 #pragma unroll
-            for (int round = 0; round < 4 / LDC; ++round) {
-                __syncwarp();
+            for (int hc = 0; hc < 2 / CS; ++hc) {
+                const int half = cs + hc;
+                const int64_t row0 = phys_wide(u) * WIDE + half * TILE;
+                const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + half * TILE);
 #pragma unroll
-                for (int c = 0; c < LDC; ++c)
-                    tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
-                tc::tmem_wait_ld();
-                if (round == 4 / LDC - 1) {
-                    tc::tc_fence_before();
+                for (int round = 0; round < 4 / LDC; ++round) {
                     __syncwarp();
-                    if (lane == 0) {
-                        if (rank == 0) tc::mbar_arrive(&acc_empty[b]);
-                        else tc::mbar_arrive_cluster(r_pacc0 + uint32_t(b * 8));
-                    }
-                }
 #pragma unroll
-                for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+                    for (int c = 0; c < LDC; ++c)
+                        tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
+                    tc::tmem_wait_ld();
+                    if (hc == 2 / CS - 1 && round == 4 / LDC - 1) {
+                        tc::tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) {
+                            if (rank == 0) tc::mbar_arrive(&acc_empty[b]);
+                            else tc::mbar_arrive_cluster(r_pacc0 + uint32_t(b * 8));
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+                }
             }
         }
         T.top = heap_drain_raw<MC == MC_DOT>(T.heap, T.cbuf, a.kk, hs, T.nbuf, T.top, a.perm);
@@ -1031,11 +1041,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads<1>(), 1)
 // Launches the pair scan over all query tiles (rounded up to an even count:
 // the query tile sets are allocated in pairs), `wave` query tiles per launch
 // (0: one launch; rounded up to an even count).
-template <int KST, int MC>
+template <int KST, int MC, int CS>
 cudaError_t launch_pair_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *launches) {
-    size_t smem = PairSmem<KST>::total(a.kp, a.kk);
+    size_t smem = PairSmem<KST, CS>::total(a.kp, a.kk);
     if (smem < kAloneSmem) smem = kAloneSmem;  // all 512 TMEM columns: alone on the SM
-    auto kern = tc_pair_kernel<KST, MC>;
+    auto kern = tc_pair_kernel<KST, MC, CS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     CUtensorMap dmap;
@@ -1047,7 +1057,7 @@ cudaError_t launch_pair_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *l
         TcArgs b = a;
         b.qt0 = t0;
         dim3 grid(unsigned(std::min<int64_t>(per, qtiles - t0)), unsigned(a.splits));
-        kern<<<grid, tc_threads<1>(), smem, st>>>(b, dmap);
+        kern<<<grid, 64 + TILE * CS, smem, st>>>(b, dmap);
         if (launches) *launches += 1;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -1055,11 +1065,11 @@ cudaError_t launch_pair_t(const TcArgs &a, cudaStream_t st, int64_t wave, int *l
     return cudaSuccess;
 }
 
-template <int KST>
+template <int KST, int CS = 2>
 cudaError_t launch_pair_mc(const TcArgs &a, int mc, cudaStream_t st, int64_t wave, int *launches) {
-    if (mc == MC_SQ) return launch_pair_t<KST, MC_SQ>(a, st, wave, launches);
-    if (mc == MC_COS) return launch_pair_t<KST, MC_COS>(a, st, wave, launches);
-    return launch_pair_t<KST, MC_DOT>(a, st, wave, launches);
+    if (mc == MC_SQ) return launch_pair_t<KST, MC_SQ, CS>(a, st, wave, launches);
+    if (mc == MC_COS) return launch_pair_t<KST, MC_COS, CS>(a, st, wave, launches);
+    return launch_pair_t<KST, MC_DOT, CS>(a, st, wave, launches);
 }
 
 // thr[q] = the smallest over the query's segments of the segment's last
@@ -1210,6 +1220,20 @@ bool pair_choose(int kp, int kk, int *kst) {
     if (PairSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
     return false;
 }
+// Ring depth of the one-heap-per-query pair scan (long candidate lists).
+bool pair1_choose(int kp, int kk, int *kst) {
+    if (PairSmem<12, 1>::total(kp, kk) <= kMaxSmem) { *kst = 12; return true; }
+    if (PairSmem<10, 1>::total(kp, kk) <= kMaxSmem) { *kst = 10; return true; }
+    if (PairSmem<8, 1>::total(kp, kk) <= kMaxSmem) { *kst = 8; return true; }
+    if (PairSmem<6, 1>::total(kp, kk) <= kMaxSmem) { *kst = 6; return true; }
+    if (PairSmem<4, 1>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
+    return false;
+}
+bool tc_long_fits(int kp, int kk) {
+    int kst = 0;
+    return pair1_choose(kp, kk, &kst);
+}
+
 bool wide_choose(int kp, int kk, int *kst) {
     if (WideSmem<5>::total(kp, kk) <= kMaxSmem) { *kst = 5; return true; }
     if (WideSmem<4>::total(kp, kk) <= kMaxSmem) { *kst = 4; return true; }
@@ -1348,6 +1372,36 @@ cudaError_t launch_tc_scan(int metric, const uint8_t *q_tiles, const uint8_t *d_
     if (stages == 4) return launch_tc_mc<1, 4>(a, mc, st);
     if (stages == 3) return launch_tc_mc<1, 3>(a, mc, st);
     return launch_tc_mc<1, 2>(a, mc, st);
+}
+
+cudaError_t launch_tc_scan_long(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,
+                                int64_t n, int64_t m, int64_t dim, int kk, int splits, uint64_t *cand, int *err,
+                                cudaStream_t st, int *launches, const uint32_t *perm, const int *rot, int64_t wave,
+                                uint32_t *qbound) {
+    TcArgs a{};
+    a.qt = q_tiles;
+    a.dt = d_tiles;
+    a.dnorm = d_norm;
+    a.n = n;
+    a.m = m;
+    a.kp = tc_padded_k(dim);
+    a.kk = kk;
+    a.splits = splits;
+    a.n_tiles = tc_tiles(n);
+    a.split_tiles = (a.n_tiles + splits - 1) / splits;
+    a.cand = cand;
+    a.err = err;
+    a.perm = perm;
+    a.rot = rot;
+    a.qbound = qbound;
+    int kst = 0;
+    if (!pair1_choose(a.kp, kk, &kst)) return cudaErrorInvalidValue;
+    const int mc = metric_class(metric);
+    if (kst == 12) return launch_pair_mc<12, 1>(a, mc, st, wave, launches);
+    if (kst == 10) return launch_pair_mc<10, 1>(a, mc, st, wave, launches);
+    if (kst == 8) return launch_pair_mc<8, 1>(a, mc, st, wave, launches);
+    if (kst == 6) return launch_pair_mc<6, 1>(a, mc, st, wave, launches);
+    return launch_pair_mc<4, 1>(a, mc, st, wave, launches);
 }
 
 cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, uint32_t *pivot, int *count,

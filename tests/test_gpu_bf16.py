@@ -261,7 +261,8 @@ def test_bf16_filter_overflow_falls_back_to_exact_scan(ss):
     rng = np.random.default_rng(3)
     X = np.tile(rng.standard_normal((1, 48), dtype=np.float32), (20000, 1))
     Q = rng.standard_normal((9, 48), dtype=np.float32)
-    idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.0)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.0,
+                                 long_lists=0)
     ids, dists = ss.searchbatch(idx, ss.GenericContext(), ss.MatrixDatabase.from_rows(Q), 100)
     assert idx.get_param("fallbacks") == 9
     ri, rd = O.searchbatch("sql2", X, Q, 100)
@@ -280,3 +281,31 @@ def test_bf16_allknn_large_k(ss):
     fi, _ = O.searchbatch_f64("normcosine", X, X[rows], 121)
     gold = np.array([[i for i in fi[r] if i != j + 1][:120] for r, j in enumerate(rows)], dtype=np.uint32)
     assert O.macrorecall(gold, gi[rows]) >= 0.99
+
+
+@pytest.mark.parametrize("name,d,k,of", [("normcosine", 96, 32, 4.0), ("sql2", 64, 100, 1.0), ("ip", 128, 48, 2.0)])
+def test_bf16_long_lists_equal_threshold_filter(ss, name, d, k, of):
+    # lists too long for two heaps per query (C2 as written: 4 (k + 1) = 132
+    # candidates): CTA pairs with one heap per query keep exactly the kk
+    # best approximate keys, as the threshold filter does
+    rng = np.random.default_rng(d + k + 5)
+    X = mixture(rng, 20000, d, normalise=(name == "normcosine"))
+    Q = X[rng.integers(0, 20000, size=257)] + rng.standard_normal((257, d), dtype=np.float32) * 0.02
+    if name == "normcosine":
+        Q /= np.linalg.norm(Q, axis=1, keepdims=True)
+    li, ld = run(ss, name, X, Q, k, overfetch=of, long_lists=1)
+    fi, fd = run(ss, name, X, Q, k, overfetch=of, long_lists=0)
+    assert np.array_equal(li, fi) and np.array_equal(ld, fd)
+    check_reported_distances_exact(name, X, Q[:10], li[:10], ld[:10])
+
+
+def test_bf16_long_lists_allknn_locality(ss):
+    rng = np.random.default_rng(91)
+    X = mixture(rng, 40000, 96)
+    idx = ss.GPUExhaustiveSearch(ss.Dist.NormCosine(), ss.MatrixDatabase.from_rows(X), precision="bf16",
+                                 overfetch=4.0)
+    ctx = ss.GenericContext(logger=None)
+    ids, dists = ss.allknn(idx, ctx, 32, exclude_self=True)
+    idx.set_param("long_lists", 0)
+    fi, fd = ss.allknn(idx, ctx, 32, exclude_self=True)
+    assert np.array_equal(ids, fi) and np.array_equal(dists, fd)
