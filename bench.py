@@ -555,12 +555,12 @@ def gpu_arm(args):
     four_k = None
     if mode == "bf16" and cx.world == 1 and not args.no_plain:
         # the configuration as written: FP32 rerank of the top 4k candidates
-        # (over-fetch 4 x (k+1) = 132 per object: beyond the on-chip heaps, so
-        # the threshold-filter scan answers)
+        # (over-fetch 4 x (k+1) = 132 per object: beyond two heaps per object,
+        # so CTA pairs keep one heap per object)
         four_k = allknn_mode(cx, X, "bf16", 4.0, 3, 1)
         modes["bf16_4k"] = {"value": four_k["qps"], "ms_per_step": four_k["ms_per_step"], "overfetch": 4.0,
                             "steps": 3, "warmup": 1, "roofline": four_k["roofline"],
-                            "note": "rerank of the top 4k = 132 candidates per object, threshold-filter scan"}
+                            "note": "rerank of the top 4k = 132 candidates per object; the scan keeps them in one heap per object on CTA pairs"}
     suite = None
     if cx.world == 1 and args.suite != "none":
         suite = run_suite(cx, args)
