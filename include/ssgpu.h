@@ -150,8 +150,12 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * BF16/FP8 index, e.g. to calibrate "overfetch" against it), "profile"
  * (1 = time the scan kernel with events), "graphs" (0 = no CUDA-graph replay
  * in ssg_search_batches), "wide" (0 = BF16 scans in 128 x 128 tiles instead
- * of 128 x 256), "locality" (0 = BF16 allknn scans in id order instead of
- * the pivot-grouped order; results are identical either way), "plain_tc"
+ * of 128 x 256), "pair" (1 = BF16 / split scans on CTA pairs with M = 256
+ * MMAs), "long_lists" (0 = BF16 candidate lists too long for two heaps per
+ * query go through the threshold filter instead of CTA pairs with one heap
+ * per query; same candidates), "locality" (0 = BF16 allknn scans in id order
+ * instead of the pivot-grouped order; results are identical either way),
+ * "plain_tc"
  * (0 = keep the plain method on the CUDA cores; by default SqL2, L2,
  * NormCosine and InnerProduct over at least 4096 objects run it on the
  * tensor cores: a two-piece BF16 scan -- query tiles resident for
