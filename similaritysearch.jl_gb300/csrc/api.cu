@@ -355,7 +355,7 @@ int validate_create(int metric, int elem, int64_t dim, int64_t n, int64_t ld, in
         return fail(nullptr, SSG_EINVAL, "database length %lld out of range", (long long)n);
     if (ld < dim) return fail(nullptr, SSG_EINVAL, "leading dimension %lld < dim %lld", (long long)ld, (long long)dim);
     if (prec != SSG_PREC_FP32 && prec != SSG_PREC_BF16 && prec != SSG_PREC_FP8)
-        return fail(nullptr, SSG_EUNSUPPORTED, "precision mode %d is not available in this build", prec);
+        return fail(nullptr, SSG_EUNSUPPORTED, "precision mode %d is not supported", prec);
     if (prec != SSG_PREC_FP32 && metric == SSG_METRIC_HAMMING)
         return fail(nullptr, SSG_EUNSUPPORTED, "Hamming distances are integers: only the exact mode exists");
     return SSG_OK;
