@@ -156,9 +156,8 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * per query; same candidates), "locality" (0 = BF16 allknn scans in id order
  * instead of the pivot-grouped order; results are identical either way),
  * "plain_tc"
- * (0 = keep the plain method on the CUDA cores; by default SqL2, L2,
- * NormCosine and InnerProduct over at least 4096 objects run it on the
- * tensor cores: a two-piece BF16 scan -- query tiles resident for
+ * (0 = keep the plain method on the CUDA cores; by default the float
+ * metrics over at least 4096 objects run it on the tensor cores: a two-piece BF16 scan -- query tiles resident for
  * dim <= 128, both operands streamed along K beyond -- whose candidates are
  * re-scored in exact FP32 and certified complete, uncertified queries
  * recomputed by the exact scan; results identical either way).  Unknown

@@ -759,7 +759,7 @@ struct PlainTcPlan {
 PlainTcPlan plain_tc_plan(const ssg_index *idx, int take) {
     const int metric = idx->metric;
     if (metric != SSG_METRIC_SQL2 && metric != SSG_METRIC_L2 && metric != SSG_METRIC_NORMCOSINE &&
-        metric != SSG_METRIC_IP)
+        metric != SSG_METRIC_IP && metric != SSG_METRIC_COSINE)
         return {};
     const int k3 = 3 * ssg::tc_padded_k(idx->dim);
     if (k3 > 384) return {};
@@ -806,7 +806,9 @@ int ensure_plain_tiles(ssg_index *idx, bool query_role) {
                                       &idx->last_launches, nullptr, 1),
                "building split database tiles");
         SSG_CK(idx->ps_norm.ensure(size_t(tiles) * 128 * 4), "allocating split tile norms");
-        SSG_CK(ssg::launch_tc_norms(SSG_METRIC_SQL2, x, idx->n, idx->dim, tiles * 128,
+        // |x|^2 per row for the squared-distance and dot keys, 1 / |x| for Cosine's
+        SSG_CK(ssg::launch_tc_norms(idx->metric == SSG_METRIC_COSINE ? SSG_METRIC_COSINE : SSG_METRIC_SQL2, x,
+                                    idx->n, idx->dim, tiles * 128,
                                     static_cast<float *>(idx->ps_norm.p), idx->stream, &idx->last_launches),
                "computing split tile norms");
         SSG_RC(ensure_max_norm(idx));
@@ -829,8 +831,8 @@ constexpr int64_t kLocalityMinRows = 32768;
 
 int ensure_plain_locality(ssg_index *idx);
 
-int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
-                 float *d_dists, bool queries_are_db, const PlainTcPlan &plan) {
+int run_plain_tc(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                 uint32_t *d_ids, float *d_dists, bool queries_are_db, const PlainTcPlan &plan) {
     const int kk = plan.h, k3 = plan.k3;
     const bool sq = is_sq_metric(idx->metric);
     const int kp = ssg::tc_padded_k(idx->dim);
@@ -916,15 +918,17 @@ int run_plain_tc(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_
         f.out_dists = d_dists + size_t(c0) * k;
         f.n_rows = idx->n;
         f.rerank = std::min(plan.rr, f.segs * kk);
-        f.check = sq ? 1 : 2;
+        f.check = sq ? 1 : (idx->metric == SSG_METRIC_COSINE ? 3 : 2);
         f.q_sq = qsq;
         f.max_x_sq = idx->max_x_sq;
-        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c : c + float(idx->dim + 2) * ulp24;
+        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c
+                         : (f.check == 3 ? c + float(2 * idx->dim + 16) * ulp24 : c + float(idx->dim + 2) * ulp24);
         f.n_total = idx->n;
         f.flags = flags + c0;
         f.flag_count = flag_count;
         SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
-                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc, nullptr,
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc,
+                                           dqn ? dqn + c0 : nullptr,
                                            idx->stream, &idx->last_launches),
                "launching the rerank kernel");
         SSG_RC(timer.collect());
@@ -977,11 +981,11 @@ int ensure_plain_stream_tiles(ssg_index *idx, bool query_role) {
     return SSG_OK;
 }
 
-int run_plain_stream(ssg_index *idx, const float *dq, int64_t m, int k, int exclude_self, uint32_t *d_ids,
-                     float *d_dists, bool queries_are_db) {
+int run_plain_stream(ssg_index *idx, const float *dq, const float *dqn, int64_t m, int k, int exclude_self,
+                     uint32_t *d_ids, float *d_dists, bool queries_are_db) {
     const int metric = idx->metric;
     if (metric != SSG_METRIC_SQL2 && metric != SSG_METRIC_L2 && metric != SSG_METRIC_NORMCOSINE &&
-        metric != SSG_METRIC_IP)
+        metric != SSG_METRIC_IP && metric != SSG_METRIC_COSINE)
         return kPlainNotApplicable;
     const bool sq = is_sq_metric(metric);
     const int take = k + (exclude_self ? 1 : 0);
@@ -1059,15 +1063,17 @@ int run_plain_stream(ssg_index *idx, const float *dq, int64_t m, int k, int excl
         f.out_ids = d_ids + size_t(c0) * k;
         f.out_dists = d_dists + size_t(c0) * k;
         f.n_rows = idx->n;
-        f.check = sq ? 1 : 2;
+        f.check = sq ? 1 : (idx->metric == SSG_METRIC_COSINE ? 3 : 2);
         f.q_sq = qsq;
         f.max_x_sq = idx->max_x_sq;
-        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c : c + float(idx->dim + 2) * ulp24;
+        f.err_scale = sq ? 4.0f * float(idx->dim + 2) * ulp24 + 0.5f * c
+                         : (f.check == 3 ? c + float(2 * idx->dim + 16) * ulp24 : c + float(idx->dim + 2) * ulp24);
         f.n_total = idx->n;
         f.flags = flags + c0;
         f.flag_count = flag_count;
         SSG_CK(ssg::launch_finalize_rerank(idx->metric, f, static_cast<const float *>(idx->db.p),
-                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc, nullptr,
+                                           static_cast<const float *>(idx->db_norm.p), idx->dim, qc,
+                                           dqn ? dqn + c0 : nullptr,
                                            idx->stream, &idx->last_launches),
                "launching the rerank kernel");
         SSG_RC(timer.collect());
@@ -1108,10 +1114,10 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
         const PlainTcPlan plan = plain_tc_plan(idx, k + (exclude_self ? 1 : 0));
         idx->last_plain_tc = plan.k3 > 0;
         if (plan.k3 > 0)
-            return run_plain_tc(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
+            return run_plain_tc(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
                                 queries_are_db, plan);
         if (ssg::tc_padded_k(idx->dim) > 128) {
-            const int rc = run_plain_stream(idx, static_cast<const float *>(dq), m, k, exclude_self, d_ids, d_dists,
+            const int rc = run_plain_stream(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
                                             queries_are_db);
             if (rc != kPlainNotApplicable) {
                 idx->last_plain_tc = rc == SSG_OK;
@@ -1251,7 +1257,8 @@ int ensure_plain_locality(ssg_index *idx) {
                                   &idx->last_launches, perm, 2),
            "building locality-ordered split query tiles");
     SSG_CK(idx->loc_ps_norm.ensure(size_t(tiles) * 128 * 4), "allocating locality-ordered norms");
-    SSG_CK(ssg::launch_tc_norms(SSG_METRIC_SQL2, x, n, idx->dim, tiles * 128,
+    SSG_CK(ssg::launch_tc_norms(idx->metric == SSG_METRIC_COSINE ? SSG_METRIC_COSINE : SSG_METRIC_SQL2, x, n,
+                                idx->dim, tiles * 128,
                                 static_cast<float *>(idx->loc_ps_norm.p), idx->stream, &idx->last_launches, perm),
            "computing locality-ordered norms");
     SSG_CK(cudaStreamSynchronize(idx->stream), "building locality-ordered split tiles");

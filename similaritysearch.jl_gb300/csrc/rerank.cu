@@ -124,7 +124,11 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
         //           |y| <= ((1 + t) |q| + sqrt(D_take)) / (1 - t), and
         //           |y| <= sqrt(max |x|^2) always;
         //   check 2 (keys -x.q): c = 1 for NormCosine, 0 for InnerProduct,
-        //           E = err_scale sqrt(max |x|^2) |q| + 2^-22.
+        //           E = err_scale sqrt(max |x|^2) |q| + 2^-22;
+        //   check 3 (Cosine's keys -x.q / |x|): distances 1 + a / |q|, so
+        //           a_low enters as 1 + a_low / |q| and E = err_scale (the
+        //           split's c plus the FP32 dot, norms, division and
+        //           subtraction, (2 d + 16) 2^-24, all relative to 1).
         // If a_low + c - E exceeds the exact distance of the take-th
         // re-ranked candidate (for L2 its square, widened by 2^-20 so that
         // sqrt rounding cannot tie), y ranks behind it: the list holds the
@@ -150,6 +154,9 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
                 const double r = xm + sqrt(qs);
                 c = qs;
                 E = double(f.err_scale) * r * r;
+            } else if (f.check == 3) {
+                c = 1.0;
+                E = double(f.err_scale);
             } else {
                 c = METRIC == NORMCOSINE ? 1.0 : 0.0;
                 E = double(f.err_scale) * xm * sqrt(qs) + 2.384185791015625e-7;
@@ -161,7 +168,8 @@ __global__ void finalize_rerank_kernel(FinalizeArgs f, const float *db, const fl
                 const double r = fmin(xm, ((1.0 + t) * sqrt(qs) + sqrt(dtake)) / (1.0 - t)) + sqrt(qs);
                 E = double(f.err_scale) * r * r;
             }
-            const double lower = certified ? double(key_dist(low)) + c - E : 0.0;
+            const double a_low = f.check == 3 ? double(key_dist(low)) / sqrt(qs) : double(key_dist(low));
+            const double lower = certified ? a_low + c - E : 0.0;
             if (!certified || !(lower > dtake)) {
                 f.flags[j] = 1;
                 atomicAdd(f.flag_count, 1);

@@ -14,7 +14,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-METRICS = {"sql2": "SqL2", "l2": "L2", "normcosine": "NormCosine", "ip": "InnerProduct"}
+METRICS = {"sql2": "SqL2", "l2": "L2", "normcosine": "NormCosine", "ip": "InnerProduct", "cosine": "Cosine"}
 
 
 @pytest.fixture(scope="module")
