@@ -1094,6 +1094,15 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
 int run_knn_stream(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, int exclude_self,
                    uint32_t *d_ids, float *d_dists, bool queries_are_db);
 
+// Frees the plain method's split tiles (and their locality-ordered copies).
+void release_plain_tiles(ssg_index *idx) {
+    for (DevBuf *b : {&idx->ps_db, &idx->ps_dbq, &idx->ps_norm, &idx->ps_q, &idx->pss_db, &idx->pss_dbq,
+                      &idx->pss_alpha, &idx->pss_beta, &idx->pss_q, &idx->loc_ps_db, &idx->loc_ps_dbq,
+                      &idx->loc_ps_norm})
+        b->release();
+    idx->ps_rows = idx->ps_qrows = idx->pss_rows = idx->pss_qrows = idx->loc_ps_n = -1;
+}
+
 // Databases below this many rows keep the plain method on the CUDA cores
 // (the split tiles would cost more than the scan they speed up).
 constexpr int64_t kPlainTcMinRows = 4096;
@@ -1111,18 +1120,21 @@ int run_knn(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int k, 
     idx->last_plain_tc = 0;
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param && idx->plain_tc_param &&
         idx->n >= kPlainTcMinRows && !idx->capturing) {
+        // the split tiles take 1.5x the FP32 database per role: when device
+        // memory runs out the CUDA-core form answers instead (it rewrites
+        // every output row)
         const PlainTcPlan plan = plain_tc_plan(idx, k + (exclude_self ? 1 : 0));
-        idx->last_plain_tc = plan.k3 > 0;
+        int rc = kPlainNotApplicable;
         if (plan.k3 > 0)
-            return run_plain_tc(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
-                                queries_are_db, plan);
-        if (ssg::tc_padded_k(idx->dim) > 128) {
-            const int rc = run_plain_stream(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
-                                            queries_are_db);
-            if (rc != kPlainNotApplicable) {
-                idx->last_plain_tc = rc == SSG_OK;
-                return rc;
-            }
+            rc = run_plain_tc(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
+                              queries_are_db, plan);
+        else if (ssg::tc_padded_k(idx->dim) > 128)
+            rc = run_plain_stream(idx, static_cast<const float *>(dq), dqn, m, k, exclude_self, d_ids, d_dists,
+                                  queries_are_db);
+        if (rc == SSG_ENOMEM) release_plain_tiles(idx);
+        else if (rc != kPlainNotApplicable) {
+            idx->last_plain_tc = 1;
+            return rc;
         }
     }
     if (idx->metric != SSG_METRIC_HAMMING && !idx->exact_scan_param) {
