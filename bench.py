@@ -797,21 +797,23 @@ def suite_c4(cx, args, data):
         metric = N.METRIC_IP if name == "ip" else N.METRIC_SQL2
         h = cx.create(metric, N.ELEM_F32, X, PREC["fp8"])
         Qd = torch.from_numpy(Q).cuda()
-        # over-fetch: the autotuner's rule on calibration queries (the
-        # stream's first 2,048) against the plain method; recall is then
-        # reported on the whole stream and on held-out queries
-        nc = min(2048, Q.shape[0])
+        # over-fetch: the autotuner's rule on 2,048 calibration queries of
+        # their own seeds (neither the timed stream nor the held-out queries)
+        # against the plain method; recall is then reported on the whole
+        # stream and on the held-out queries
+        Qc = torch.from_numpy(workloads().c4_calibration_queries(2048, d)).cuda()
+        nc = Qc.shape[0]
         ci = torch.empty((nc, 10), dtype=torch.int32, device="cuda")
         cd = torch.empty((nc, 10), dtype=torch.float32, device="cuda")
         cx.set(h, "plain", 1.0)
-        N.check(L.ssg_search_device(h, C.c_void_p(Qd.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
+        N.check(L.ssg_search_device(h, C.c_void_p(Qc.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
                                     C.c_void_p(cd.data_ptr()), 0), h)
         gold_c = ci.cpu().numpy().view(np.uint32).copy()
         cx.set(h, "plain", 0.0)
         chosen = 16.0
         for c in (1.0, 1.25, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0):
             cx.set(h, "overfetch", c)
-            N.check(L.ssg_search_device(h, C.c_void_p(Qd.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
+            N.check(L.ssg_search_device(h, C.c_void_p(Qc.data_ptr()), nc, 10, C.c_void_p(ci.data_ptr()),
                                         C.c_void_p(cd.data_ptr()), 0), h)
             if O.macrorecall(gold_c, ci.cpu().numpy().view(np.uint32)) >= 0.997:
                 chosen = c
@@ -863,7 +865,7 @@ def suite_c4(cx, args, data):
                                  C.c_void_p(oi.data_ptr()), C.c_void_p(od.data_ptr()), 0), h)
         e2e_s = time.perf_counter() - t0
         L.ssg_destroy(h)
-        del Qd, Hd, ci, cd, hi, hd
+        del Qd, Qc, Hd, ci, cd, hi, hd
         torch.cuda.empty_cache()
         cpu, _, _, _ = cpu_searchbatch_baseline(name, X, H, 10, budget_s=5.0)
         # HBM bytes one scan of the stream reads per batch (FP8 rows + the

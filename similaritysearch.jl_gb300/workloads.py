@@ -21,6 +21,8 @@ those sizes see the same data.
       round(LogNormal(ln 64, 1)) clipped to [1, 4096] (seed 13), k uniform
       over {1, 10, 100} (seed 14); queries from the same mixture (seeds 15,
       16).
+      Held-out queries (seeds 17, 18) and over-fetch calibration queries
+      (seeds 19, 20) come from the same mixture.
 * C5  the learned shortlist on the C4 database (SqL2, k = 10).
 """
 from __future__ import annotations
@@ -89,3 +91,9 @@ def c4_heldout_queries(m: int, d: int = 768) -> np.ndarray:
     """Queries from C4's mixture on seeds the request stream does not use
     (17, 18): held out from every calibration."""
     return c4_draw(m, 17, 18, d)
+
+
+def c4_calibration_queries(m: int, d: int = 768) -> np.ndarray:
+    """Queries from C4's mixture on their own seeds (19, 20), for tuning the
+    over-fetch: neither the timed request stream nor the held-out queries."""
+    return c4_draw(m, 19, 20, d)

@@ -15,8 +15,8 @@ oracle and the FP64 ranking.
   rows: recall@10 and recall@32 >= 0.99 against the FP64 ranking and every
   reported distance the exact FP32 distance of its id.
 * C4 and C5 at full n (2,000,000 x 768): recall@10 >= 0.99 against the FP64
-  ranking on held-out queries (a seed the over-fetch calibration and the
-  training never saw).
+  ranking on held-out queries (seeds the over-fetch calibration, its own
+  calibration queries, and the training never saw).
 """
 import numpy as np
 import pytest
@@ -126,19 +126,19 @@ def test_c2_bf16_allknn_recall_vs_fp64(ss, c2, overfetch):
 
 @pytest.fixture(scope="module")
 def c4(ss):
-    from similaritysearch_gb300.workloads import c4_heldout_queries, make_c4
+    from similaritysearch_gb300.workloads import c4_calibration_queries, c4_heldout_queries, make_c4
     X, Q, sizes, ks = make_c4()
-    return X, Q, c4_heldout_queries(64)
+    return X, c4_calibration_queries(2048), c4_heldout_queries(64)
 
 
 @pytest.mark.parametrize("name", ["ip", "sql2"])
 def test_c4_fp8_recall_vs_fp64_on_heldout_queries(ss, c4, name):
-    X, Q, H = c4
+    X, Qc, H = c4
     dist = ss.Dist.InnerProduct() if name == "ip" else ss.Dist.SqL2()
     idx = ss.GPUExhaustiveSearch(dist, dbq(ss, X), precision="fp8")
-    # over-fetch calibrated on the stream's first 2,048 queries against the
-    # plain method; scored on held-out queries
-    of = idx.autotune_overfetch(dbq(ss, Q[:2048]), 10, target_recall=0.997)
+    # over-fetch calibrated on 2,048 calibration queries against the plain
+    # method; scored on held-out queries
+    of = idx.autotune_overfetch(dbq(ss, Qc), 10, target_recall=0.997)
     ctx = ss.GenericContext(logger=None)
     fi, _ = O.searchbatch_f64(name, X, H, 10, nthreads=THREADS)
     for k in (10, 100):
@@ -147,7 +147,7 @@ def test_c4_fp8_recall_vs_fp64_on_heldout_queries(ss, c4, name):
 
 
 def test_c5_learned_recall_vs_fp64_on_heldout_queries(ss, c4):
-    X, Q, H = c4
+    X, _, H = c4
     idx = ss.GPUExhaustiveSearch(ss.Dist.SqL2(), dbq(ss, X))
     st = idx.train_mlp(sample=200_000, triplets=1_000_000, epochs=4, hidden=256, out_dim=64, batch=1024,
                        seed=15, target_recall=0.99)
