@@ -155,7 +155,9 @@ int ssg_rerank(ssg_index *idx, const void *host_q, int64_t m, int32_t len,
  * query go through the threshold filter instead of CTA pairs with one heap
  * per query; same candidates), "locality" (0 = BF16 allknn scans in id order
  * instead of the pivot-grouped order; results are identical either way),
- * "plain_tc"
+ * "locality_rows" (database rows per pivot of that order, 64..65536, default
+ * 128), "locality_chain" (0 = the pivots' groups in pivot order instead of a
+ * greedy nearest-pivot chain; results identical), "plain_tc"
  * (0 = keep the plain method on the CUDA cores; by default the float
  * metrics over at least 4096 objects run it on the tensor cores: a two-piece BF16 scan -- query tiles resident for
  * dim <= 128, both operands streamed along K beyond -- whose candidates are

@@ -85,9 +85,12 @@ struct ssg_index {
     DevBuf tc_db, tc_norm, tc_q, status;
     // allknn's locality order (tc_bf16.cu): position -> id, start tile of
     // each query tile's scan, BF16 tiles and norms in that order; built for
-    // loc_n rows (-1: none)
+    // loc_n rows (-1: none) from a pivot per loc_rows_param rows, the groups
+    // in the pivots' chain order (loc_chain_param) or in pivot order
     DevBuf loc_perm, loc_rot, loc_tiles, loc_norm;
     int64_t loc_n = -1, loc_bf16_n = -1;
+    int64_t loc_rows_param = 128;
+    int loc_chain_param = 1;
     // the plain method's split tiles (both roles) and |x|^2 in that order,
     // built for loc_ps_n rows (-1: none)
     DevBuf loc_ps_db, loc_ps_dbq, loc_ps_norm;
@@ -1164,18 +1167,107 @@ int64_t overfetch_kk(const ssg_index *idx, int take) {
     return std::min<int64_t>(kk64, std::max<int64_t>(take, std::min<int64_t>(idx->n, 4096)));
 }
 
+// The pivots' chain order: rank[p] = place of pivot p in a greedy chain
+// that starts at pivot 0 and always links the nearest pivot not yet linked
+// among the last link's kNear nearest pivots (a BF16 scan of the pivots
+// against themselves), else among the lists of the links before it, else the
+// lowest-numbered pivot left.  Pivots near each other so take nearby places,
+// and the groups of one dense region of the data sit side by side.  Leaves
+// rank empty when the pivots' scan does not fit (the groups then keep pivot
+// order).
+int pivot_chain(ssg_index *idx, const uint32_t *pmap, int P, DevBuf &rank) {
+    constexpr int kNear = 16;
+    const int kk = std::min(kNear + 1, P);  // the pivot itself comes first
+    const int64_t tiles = (ssg::tc_tiles(P) + 1) / 2 * 2;
+    const float *x = static_cast<const float *>(idx->db.p);
+    DevBuf t, nrm, keys;
+    SSG_CK(t.ensure(size_t(tiles) * ssg::tc_tile_bytes(idx->dim)), "allocating pivot tiles");
+    SSG_CK(nrm.ensure(size_t(tiles) * 128 * 4), "allocating pivot norms");
+    SSG_CK(ssg::launch_bf16_tiles(x, P, idx->dim, tiles, static_cast<uint8_t *>(t.p), idx->stream,
+                                  &idx->last_launches, pmap, 0),
+           "building pivot tiles");
+    SSG_CK(ssg::launch_tc_norms(idx->metric, x, P, idx->dim, tiles * 128, static_cast<float *>(nrm.p), idx->stream,
+                                &idx->last_launches, pmap),
+           "computing pivot norms");
+    const int max_segs = std::max(ssg::tc_segments_per_split(1), ssg::tc_segments_per_split(2));
+    SSG_CK(keys.ensure(size_t(P) * max_segs * kk * 8), "allocating pivot neighbour lists");
+    SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
+    int qt = 1;
+    const cudaError_t e = ssg::launch_tc_scan(idx->metric, static_cast<const uint8_t *>(t.p),
+                                              static_cast<const uint8_t *>(t.p), static_cast<const float *>(nrm.p), P, P,
+                                              idx->dim, kk, 1, static_cast<uint64_t *>(keys.p),
+                                              static_cast<int *>(idx->status.p), idx->stream, &idx->last_launches, &qt,
+                                              nullptr, nullptr, true);
+    if (e == cudaErrorInvalidValue) return SSG_OK;  // no tile shape fits (nothing launched): pivot order
+    SSG_CK(e, "launching the pivots' scan");
+    const int segs = ssg::tc_segments_per_split(qt);
+    std::vector<uint64_t> h(size_t(P) * segs * kk);
+    int status = 0;
+    SSG_CK(cudaMemcpyAsync(h.data(), keys.p, h.size() * 8, cudaMemcpyDeviceToHost, idx->stream),
+           "reading pivot neighbour lists");
+    SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
+           "reading the status word");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "scanning the pivots");
+    if (status != 0)
+        return fail(idx, SSG_ETIMEOUT, "a bounded wait in the pivots' scan gave up (code %d)", status);
+    // each pivot's nearest other pivots, nearest first
+    std::vector<uint32_t> near(size_t(P) * kNear, UINT32_MAX);
+    std::vector<uint64_t> row(size_t(segs) * kk);
+    for (int p = 0; p < P; ++p) {
+        std::copy(h.begin() + size_t(p) * row.size(), h.begin() + size_t(p + 1) * row.size(), row.begin());
+        std::sort(row.begin(), row.end());
+        int c = 0;
+        for (size_t i = 0; i < row.size() && c < kNear; ++i) {
+            if (row[i] == ssg::KEY_EMPTY) break;
+            const uint32_t q = ssg::key_id0(row[i]);
+            if (q == uint32_t(p) || q >= uint32_t(P)) continue;
+            near[size_t(p) * kNear + c++] = q;
+        }
+    }
+    std::vector<uint32_t> place(size_t(P), UINT32_MAX), chain;
+    chain.reserve(size_t(P));
+    place[0] = 0;
+    chain.push_back(0);
+    int lowest = 1;
+    for (int r = 1; r < P; ++r) {
+        uint32_t next = UINT32_MAX;
+        // the last link's list, then those of up to 64 links before it
+        for (int back = 0; back < 65 && back < r && next == UINT32_MAX; ++back) {
+            const uint32_t *lst = near.data() + size_t(chain[size_t(r - 1 - back)]) * kNear;
+            for (int i = 0; i < kNear; ++i)
+                if (lst[i] != UINT32_MAX && place[lst[i]] == UINT32_MAX) {
+                    next = lst[i];
+                    break;
+                }
+        }
+        if (next == UINT32_MAX) {
+            while (place[size_t(lowest)] != UINT32_MAX) ++lowest;
+            next = uint32_t(lowest);
+        }
+        place[next] = uint32_t(r);
+        chain.push_back(next);
+    }
+    SSG_CK(rank.ensure(size_t(P) * 4), "allocating pivot ranks");
+    SSG_CK(cudaMemcpyAsync(rank.p, place.data(), size_t(P) * 4, cudaMemcpyHostToDevice, idx->stream),
+           "copying pivot ranks");
+    SSG_CK(cudaStreamSynchronize(idx->stream), "copying pivot ranks");
+    return SSG_OK;
+}
+
 // Builds allknn's locality order (tc_bf16.cu, launch_locality_order): P
-// evenly spaced rows as pivots (about 1024 rows per pivot), each row's
+// evenly spaced rows as pivots (one per loc_rows_param rows), each row's
 // nearest pivot by a kk = 1 scan of the database's tiles in the query role
 // (`qtiles`: the BF16 tiles, or the plain method's split tiles with `split`
-// 2) against the pivots' tiles, rows grouped by pivot; position -> id in
-// loc_perm and each query tile's start tile in loc_rot.  The order only
-// groups rows: any assignment to pivots gives the same results.  Kept until
-// the database changes.
+// 2) against the pivots' tiles, rows grouped by pivot, the groups in the
+// pivots' chain order (pivot_chain); position -> id in loc_perm and each
+// query tile's start tile in loc_rot.  The order only groups rows: any
+// assignment to pivots and any group order give the same results.  Kept
+// until the database or the parameters change.
 int ensure_locality_order(ssg_index *idx, const uint8_t *qtiles, int split) {
     if (idx->loc_n == idx->n) return SSG_OK;
     const int64_t n = idx->n;
-    const int P = int(std::min<int64_t>(16384, std::max<int64_t>(128, (n / 1024 + 127) / 128 * 128)));
+    const int64_t per = idx->loc_rows_param;
+    const int P = int(std::min<int64_t>(16384, std::max<int64_t>(128, (n / per + 127) / 128 * 128)));
     std::vector<uint32_t> prow(static_cast<size_t>(P));
     for (int i = 0; i < P; ++i) prow[size_t(i)] = uint32_t(int64_t(i) * n / P);
     const int64_t kdim = split ? 3 * ssg::tc_padded_k(idx->dim) : idx->dim;
@@ -1196,6 +1288,9 @@ int ensure_locality_order(ssg_index *idx, const uint8_t *qtiles, int split) {
     SSG_CK(ssg::launch_tc_norms(idx->metric, x, P, idx->dim, ptiles * 128, static_cast<float *>(pn.p), idx->stream,
                                 &idx->last_launches, pmap),
            "computing pivot norms");
+    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
+    DevBuf rank;
+    if (idx->loc_chain_param) SSG_RC(pivot_chain(idx, pmap, P, rank));
     // nearest pivot of every row (its keys), then per-row pivot, bucket
     // counts, starts and cursors in one scratch buffer
     const size_t cand_bytes = size_t(n) * segs * 8;
@@ -1203,7 +1298,6 @@ int ensure_locality_order(ssg_index *idx, const uint8_t *qtiles, int split) {
     uint64_t *cand = static_cast<uint64_t *>(work.p);
     uint32_t *pivot = reinterpret_cast<uint32_t *>(static_cast<char *>(work.p) + cand_bytes);
     int *count = reinterpret_cast<int *>(pivot + n);
-    SSG_CK(idx->status.ensure(sizeof(int)), "allocating the status word");
     SSG_CK(cudaMemsetAsync(idx->status.p, 0, sizeof(int), idx->stream), "clearing the status word");
     // the split tiles' K only fits the wide scan
     SSG_CK(ssg::launch_tc_scan(idx->metric, qtiles, static_cast<const uint8_t *>(pt.p),
@@ -1214,9 +1308,9 @@ int ensure_locality_order(ssg_index *idx, const uint8_t *qtiles, int split) {
     const int64_t qtiles_n = ssg::tc_tiles(n);
     SSG_CK(idx->loc_perm.ensure(size_t(n) * 4), "allocating the locality order");
     SSG_CK(idx->loc_rot.ensure(size_t(qtiles_n) * 4), "allocating scan start tiles");
-    SSG_CK(ssg::launch_locality_order(cand, n, segs, P, pivot, count, count + P, count + 2 * P,
-                                      static_cast<uint32_t *>(idx->loc_perm.p), static_cast<int *>(idx->loc_rot.p),
-                                      idx->stream, &idx->last_launches),
+    SSG_CK(ssg::launch_locality_order(cand, n, segs, P, static_cast<const uint32_t *>(rank.p), pivot, count,
+                                      count + P, count + 2 * P, static_cast<uint32_t *>(idx->loc_perm.p),
+                                      static_cast<int *>(idx->loc_rot.p), idx->stream, &idx->last_launches),
            "ordering rows by pivot");
     int status = 0;
     SSG_CK(cudaMemcpyAsync(&status, idx->status.p, sizeof(int), cudaMemcpyDeviceToHost, idx->stream),
@@ -2199,6 +2293,14 @@ int ssg_set_param(ssg_index *idx, const char *key, double value) {
         idx->pair_param = value != 0.0;
     } else if (k == "long_lists") {
         idx->long_param = value != 0.0;
+    } else if (k == "locality_rows" || k == "locality_chain") {
+        if (k == "locality_rows") {
+            if (!(value >= 64 && value <= 65536)) return fail(idx, SSG_EINVAL, "locality_rows out of range");
+            idx->loc_rows_param = int64_t(value);
+        } else {
+            idx->loc_chain_param = value != 0.0;
+        }
+        idx->loc_n = idx->loc_bf16_n = idx->loc_ps_n = -1;  // rebuilt on the next allknn
     } else if (k == "wave") {
         if (!(value >= 0 && value <= 1e6)) return fail(idx, SSG_EINVAL, "wave out of range");
         idx->wave_param = int64_t(value);
@@ -2237,6 +2339,8 @@ int ssg_get_param(ssg_index *idx, const char *key, double *value) {
     else if (k == "plain") *value = idx->plain_param;
     else if (k == "plain_tc") *value = idx->plain_tc_param;
     else if (k == "long_lists") *value = idx->long_param;
+    else if (k == "locality_rows") *value = double(idx->loc_rows_param);
+    else if (k == "locality_chain") *value = idx->loc_chain_param;
     else if (k == "last_plain_tc") *value = idx->last_plain_tc;
     else if (k == "learned") *value = idx->learned_param;
     else if (k == "learned_target") *value = idx->learned_target;

@@ -156,11 +156,13 @@ cudaError_t launch_tc_scan_long(int metric, const uint8_t *q_tiles, const uint8_
                                 cudaStream_t st, int *launches, const uint32_t *perm, const int *rot, int64_t wave,
                                 uint32_t *qbound);
 // Locality order from a kk = 1 scan of n rows against P pivots (cand: n x
-// segs keys): pivot[i], bucket counts / starts, perm (position -> row, rows
-// grouped by pivot) and rot (start tile of each query tile's scan).
-cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, uint32_t *pivot, int *count,
-                                  int *start, int *cursor, uint32_t *perm, int *rot, cudaStream_t st,
-                                  int *launches);
+// segs keys): pivot[i] (the bucket: rank[pivot], or the pivot itself with
+// rank null), bucket counts / starts, perm (position -> row, rows grouped by
+// bucket) and rot (start tile of each query tile's scan: its first row's
+// group).
+cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, const uint32_t *rank,
+                                  uint32_t *pivot, int *count, int *start, int *cursor, uint32_t *perm, int *rot,
+                                  cudaStream_t st, int *launches);
 // Threshold-filter scan for candidate counts beyond the on-chip heaps: every
 // (query, row) with d~ <= thr[query] is appended to the query's fcap-key list.
 cudaError_t launch_tc_filter(int metric, const uint8_t *q_tiles, const uint8_t *d_tiles, const float *d_norm,

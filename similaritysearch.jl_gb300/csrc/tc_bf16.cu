@@ -1114,22 +1114,27 @@ __global__ void filter_select_kernel(const uint64_t *__restrict__ fout, const in
 
 // ---------------------------------------------------------------------------
 // Locality order for allknn.  Rows are grouped by their nearest pivot (P
-// evenly spaced database rows), so a query tile's near neighbours sit in a
-// few consecutive database tiles, and each query CTA starts its scan there.
-// The heaps then hold close candidates after a few tiles and later tiles
-// rarely pass the frontier: far fewer heap insertions than in id order,
-// where the frontier only tightens as ~kk * ln(columns seen).  The kept
-// (distance, id) keys, and so the results, do not depend on the order.
+// evenly spaced database rows) and the groups follow the pivots' chain
+// order (pivots near each other in nearby places), so a query tile's near
+// neighbours sit in its own group and the few after it, and each query CTA
+// starts its scan at its group.  The heaps then hold close
+// candidates after a few tiles and later tiles rarely pass the frontier: far
+// fewer heap insertions than in id order, where the frontier only tightens
+// as ~kk * ln(columns seen).  The kept (distance, id) keys, and so the
+// results, do not depend on the order.
 // ---------------------------------------------------------------------------
-// pivot[i] = position (0..P-1) of row i's best pivot among its segment keys
-// (a kk = 1 scan of the rows against the pivots); count[pivot] += 1
+// pivot[i] = bucket of row i: the chain place rank[p] (or p itself, rank
+// null) of its best pivot p among its segment keys (a kk = 1 scan of the
+// rows against the pivots); count[bucket] += 1
 __global__ void nearest_pivot_kernel(const uint64_t *__restrict__ cand, int64_t n, int segs,
-                                     uint32_t *__restrict__ pivot, int *__restrict__ count) {
+                                     const uint32_t *__restrict__ rank, uint32_t *__restrict__ pivot,
+                                     int *__restrict__ count) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint64_t best = KEY_EMPTY;
     for (int s = 0; s < segs; ++s) best = min(best, cand[size_t(i) * segs + s]);
-    const uint32_t p = best == KEY_EMPTY ? 0u : key_id0(best);
+    uint32_t p = best == KEY_EMPTY ? 0u : key_id0(best);
+    if (rank) p = rank[p];
     pivot[i] = p;
     atomicAdd(count + p, 1);
 }
@@ -1404,14 +1409,14 @@ cudaError_t launch_tc_scan_long(int metric, const uint8_t *q_tiles, const uint8_
     return launch_pair_mc<4, 1>(a, mc, st, wave, launches);
 }
 
-cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, uint32_t *pivot, int *count,
-                                  int *start, int *cursor, uint32_t *perm, int *rot, cudaStream_t st,
-                                  int *launches) {
+cudaError_t launch_locality_order(const uint64_t *cand, int64_t n, int segs, int P, const uint32_t *rank,
+                                  uint32_t *pivot, int *count, int *start, int *cursor, uint32_t *perm, int *rot,
+                                  cudaStream_t st, int *launches) {
     if (P < 1 || P > 1024 * 64) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(count, 0, size_t(P) * sizeof(int), st);
     if (e != cudaSuccess) return e;
     const unsigned nb = unsigned((n + 255) / 256);
-    nearest_pivot_kernel<<<nb, 256, 0, st>>>(cand, n, segs, pivot, count);
+    nearest_pivot_kernel<<<nb, 256, 0, st>>>(cand, n, segs, rank, pivot, count);
     bucket_offsets_kernel<<<1, 1024, 0, st>>>(count, P, start, cursor);
     bucket_scatter_kernel<<<nb, 256, 0, st>>>(pivot, n, cursor, perm);
     const int64_t qtiles = tc_tiles(n);

@@ -150,6 +150,29 @@ def test_bf16_allknn_locality_order_identical(ss, name):
     assert O.macrorecall(gold, gi) >= 0.98
 
 
+@pytest.mark.parametrize("rows,chain,name", [(64, 1, "normcosine"), (1024, 0, "normcosine"), (1024, 1, "sql2"),
+                                            (128, 1, "cosine")])
+def test_bf16_allknn_locality_chain_variants(ss, rows, chain, name):
+    # the pivots' chain order and the group size (rows per pivot) only
+    # reorder the scan: the results equal the id-order scan's exactly, with
+    # duplicated rows in different groups and a partial last tile
+    rng = np.random.default_rng(rows + chain)
+    n, d = 33001, 64
+    X = mixture(rng, n, d, centres=200, normalise=(name != "sql2"))
+    X[100:300] = X[20000:20200]
+    dist = getattr(ss.Dist, NAMES[name])()
+    idx = ss.GPUExhaustiveSearch(dist, ss.MatrixDatabase.from_rows(X), precision="bf16", overfetch=1.5)
+    idx.set_param("locality", 0)
+    ids_p, dists_p = ss.allknn(idx, ss.GenericContext(), 12, exclude_self=True)
+    idx.set_param("locality", 1)
+    idx.set_param("locality_rows", rows)
+    idx.set_param("locality_chain", chain)
+    assert idx.get_param("locality_rows") == rows and idx.get_param("locality_chain") == chain
+    ids_l, dists_l = ss.allknn(idx, ss.GenericContext(), 12, exclude_self=True)
+    assert np.array_equal(ids_l, ids_p)
+    assert np.array_equal(dists_l, dists_p)
+
+
 @pytest.mark.parametrize("d,k,name", [(96, 50, "normcosine"), (256, 10, "sql2"), (32, 1, "ip"), (200, 20, "cosine")])
 def test_bf16_wide_equals_narrow(ss, d, k, name):
     # the wide scan (128 x 256 MMAs, K-block ring; at d = 96, k = 50 its

@@ -148,6 +148,12 @@ def test_plain_tc_allknn_locality_order(ss, name):
     idx.set_param("locality", 0)
     ids0, dists0 = ss.allknn(idx, ctx, 16, exclude_self=True)
     assert np.array_equal(ids, ids0) and np.array_equal(dists, dists0)
+    # groups in pivot order, one pivot per 1024 rows: the same arrays
+    idx.set_param("locality", 1)
+    idx.set_param("locality_chain", 0)
+    idx.set_param("locality_rows", 1024)
+    ids1, dists1 = ss.allknn(idx, ctx, 16, exclude_self=True)
+    assert np.array_equal(ids, ids1) and np.array_equal(dists, dists1)
     rows = np.sort(rng.choice(40000, size=200, replace=False))
     ri, rd = O.allknn_rows(name, X, 17, rows, lanes=1, nthreads=O.num_threads())
     for r, j in enumerate(rows):
