@@ -508,7 +508,7 @@ cudaError_t launch_tc_mc(const TcArgs &a, int mc, cudaStream_t st) {
 // to the ring.  Two accumulators of 128 x 256 FP32 fill all 512 TMEM
 // columns.  Roles, heaps, outputs and the locality order are those of
 // tc_scan_kernel (one query tile per CTA, two epilogue warps per TMEM lane
-// quarter, each owning half of the columns and its own heap).
+// quarter, each owning alternate 32-column chunks and its own heap).
 // ---------------------------------------------------------------------------
 constexpr int WIDE = 2 * TILE;          // database rows per wide tile
 constexpr int KBLK = TILE * SW;         // bytes of one K-block of a 128-row tile
@@ -664,22 +664,24 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
             if (!ok) break;
             tc::tc_fence_after();
             T.refresh();
-            // this warp's 128 columns, LDC 32-column loads in flight per
-            // round; the accumulator goes back to the MMA warp as soon as the
-            // last load landed (two accumulators only: the MMAs must not wait
-            // for the filtering).  DOT holds all four chunks in registers;
-            // the norm-scaled metrics need registers for the distances and
-            // take two rounds of two.
+            // this warp's 128 columns: the 32-column chunks cs, cs + 2, ...
+            // of the wide tile, so that a group of neighbouring rows in the
+            // locality order feeds both heaps of a query evenly.  LDC
+            // 32-column loads in flight per round; the accumulator goes back
+            // to the MMA warp as soon as the last load landed (two
+            // accumulators only: the MMAs must not wait for the filtering).
+            // DOT holds all four chunks in registers; the norm-scaled metrics
+            // need registers for the distances and take two rounds of two.
             constexpr int LDC = MC == MC_DOT ? 4 : 2;
-            const int64_t row0 = phys_wide(u) * WIDE + cs * TILE;
-            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * TILE);
+            const int64_t row0 = phys_wide(u) * WIDE + cs * 32;
+            const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + cs * 32);
             uint32_t r[LDC][32];
 #pragma unroll
             for (int round = 0; round < 4 / LDC; ++round) {
                 __syncwarp();
 #pragma unroll
                 for (int c = 0; c < LDC; ++c)
-                    tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
+                    tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 64), r[c]);
                 tc::tmem_wait_ld();
                 if (round == 4 / LDC - 1) {
                     tc::tc_fence_before();
@@ -687,7 +689,7 @@ __global__ void __launch_bounds__(tc_threads<1>(), 1) tc_wide_kernel(TcArgs a) {
                     if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
                 }
 #pragma unroll
-                for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+                for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 64, a.dnorm);
             }
         }
         T.top = heap_drain_raw<MC == MC_DOT>(T.heap, T.cbuf, a.kk, hs, T.nbuf, T.top, a.perm);
