@@ -65,7 +65,7 @@ OVERFETCH_LADDER = (1.25, 1.5, 1.75)
 # DRAM bytes (read + write) of one headline scan launch at n = 1e6 and
 # over-fetch 1.5, from the one-pass ncu capture summarised in
 # profiles/tc_wide_bf16_allknn.md
-HEADLINE_SCAN_TRAFFIC = 34.522e9 + 0.816e9
+HEADLINE_SCAN_TRAFFIC = 56.662e9 + 0.815e9
 HEADLINE_TRAFFIC_OVERFETCH = 1.5
 
 METRIC = "queries/s @ recall@10>=0.99 (allknn NormCosine n=1e6 d=96 k=32 excl. self)"
