@@ -880,7 +880,7 @@ int run_plain_tc(ssg_index *idx, const float *dq, const float *dqn, int64_t m, i
         perm = static_cast<const uint32_t *>(idx->loc_perm.p);
         rot = static_cast<const int *>(idx->loc_rot.p);
     }
-    // every heap of a query -- its splits and the two column halves of each
+    // every heap of a query -- its splits and the two column heaps of each
     // CTA -- shares one bound (all ones: none yet)
     uint32_t *qbound = nullptr;
     if (segs > 1) {
@@ -1432,7 +1432,7 @@ int run_knn_tc(ssg_index *idx, const void *dq, const float *dqn, int64_t m, int 
                "building BF16 query tiles");
         qtiles = static_cast<const uint8_t *>(idx->tc_q.p);
     }
-    // every heap of a query -- its splits and the two column halves of each
+    // every heap of a query -- its splits and the two column heaps of each
     // CTA -- shares one bound (all ones: none yet)
     uint32_t *qbound = nullptr;
     if (segs > 1) {

@@ -174,7 +174,7 @@ struct TcArgs {
     // query tiles, see launch_tc_scan)
     int64_t qt0;
     // heap mode: per-query bound shared by every heap of the query (all
-    // splits and column halves), indexed by query position; null: none
+    // splits and both column heaps), indexed by query position; null: none
     uint32_t *qbound;
 };
 
@@ -994,20 +994,22 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 + TILE * CS, 1)
             T.refresh();
             constexpr int LDC = MC == MC_DOT ? 4 : 2;
             uint32_t r[LDC][32];
-            // this warp's column halves of the wide tile (one with two heaps
-            // per query, both with one); the accumulator goes back after the
-            // last load of the last half
+            // this warp's halves of the wide tile, each the 32-column chunks
+            // half, half + 2, ... (one half with two heaps per query, so that
+            // a group of neighbouring rows feeds both heaps evenly; both
+            // with one); the accumulator goes back after the last load of
+            // the last half
 #pragma unroll
             for (int hc = 0; hc < 2 / CS; ++hc) {
                 const int half = cs + hc;
-                const int64_t row0 = phys_wide(u) * WIDE + half * TILE;
-                const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + half * TILE);
+                const int64_t row0 = phys_wide(u) * WIDE + half * 32;
+                const uint32_t tbase = tmem_base + (uint32_t(quarter * 32) << 16) + uint32_t(b * WIDE + half * 32);
 #pragma unroll
                 for (int round = 0; round < 4 / LDC; ++round) {
                     __syncwarp();
 #pragma unroll
                     for (int c = 0; c < LDC; ++c)
-                        tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 32), r[c]);
+                        tc::tmem_ld_32x32b_x32_async(tbase + uint32_t((round * LDC + c) * 64), r[c]);
                     tc::tmem_wait_ld();
                     if (hc == 2 / CS - 1 && round == 4 / LDC - 1) {
                         tc::tc_fence_before();
@@ -1018,7 +1020,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(64 + TILE * CS, 1)
                         }
                     }
 #pragma unroll
-                    for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 32, a.dnorm);
+                    for (int c = 0; c < LDC; ++c) T.chunk(r[c], row0 + (round * LDC + c) * 64, a.dnorm);
                 }
             }
         }
