@@ -10,6 +10,7 @@
 #include "ssgpu.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "chain.h"
 
 #include <cuda_runtime.h>
 #include <fcntl.h>
@@ -1224,29 +1225,9 @@ int pivot_chain(ssg_index *idx, const uint32_t *pmap, int P, DevBuf &rank) {
             near[size_t(p) * kNear + c++] = q;
         }
     }
-    std::vector<uint32_t> place(size_t(P), UINT32_MAX), chain;
-    chain.reserve(size_t(P));
-    place[0] = 0;
-    chain.push_back(0);
-    int lowest = 1;
-    for (int r = 1; r < P; ++r) {
-        uint32_t next = UINT32_MAX;
-        // the last link's list, then those of up to 64 links before it
-        for (int back = 0; back < 65 && back < r && next == UINT32_MAX; ++back) {
-            const uint32_t *lst = near.data() + size_t(chain[size_t(r - 1 - back)]) * kNear;
-            for (int i = 0; i < kNear; ++i)
-                if (lst[i] != UINT32_MAX && place[lst[i]] == UINT32_MAX) {
-                    next = lst[i];
-                    break;
-                }
-        }
-        if (next == UINT32_MAX) {
-            while (place[size_t(lowest)] != UINT32_MAX) ++lowest;
-            next = uint32_t(lowest);
-        }
-        place[next] = uint32_t(r);
-        chain.push_back(next);
-    }
+    // the last link's list, then those of up to 64 links before it
+    std::vector<uint32_t> place(static_cast<size_t>(P));
+    ssg::greedy_chain(near.data(), P, kNear, 64, place.data());
     SSG_CK(rank.ensure(size_t(P) * 4), "allocating pivot ranks");
     SSG_CK(cudaMemcpyAsync(rank.p, place.data(), size_t(P) * 4, cudaMemcpyHostToDevice, idx->stream),
            "copying pivot ranks");
